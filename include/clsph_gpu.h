@@ -1,0 +1,164 @@
+/* clsph_gpu.h — C ABI of the GB300 (sm_103a) SPH substep engine.
+ *
+ * This is the boundary between the reference-compatible C++ host layer
+ * (sph_simulation, scene, houdini_file_saver; include/clsph/) and the CUDA
+ * kernels. Plain C: opaque handle, plain pointers and sizes, int status.
+ * Every function returns 0 (CLSPH_OK) or a CLSPH_ERR_* code and never exits.
+ *
+ * Byte formats are the reference's own shared host/device structs:
+ *   clsph_particle     = particle                    (libclsph/common/structures.h:42-46), 80 B
+ *   clsph_parameters   = simulation_parameters       (structures.h:16-40), 128 B
+ *   clsph_kernel_terms = precomputed_kernel_values   (structures.h:48-54), 20 B
+ *
+ * One call of clsph_gpu_step(h, 1) is one call of the reference's
+ * sph_simulation::simulate_single_frame (libclsph/sph_simulation.cpp:227-398):
+ * bounding box + grid, Morton keys, stable sort, cell offsets, density and
+ * Tait pressure, internal forces, leapfrog + mesh collision. Particles stay
+ * resident in device memory between substeps; host transfers happen only in
+ * clsph_gpu_upload / clsph_gpu_download.
+ */
+#ifndef CLSPH_GPU_H
+#define CLSPH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  float s[4];
+} clsph_float3; /* cl_float3: 16 bytes, .s[3] unused */
+
+typedef struct {
+  clsph_float3 position, velocity, intermediate_velocity, acceleration;
+  float density, pressure;
+  uint32_t grid_index;
+  uint32_t padding_;
+} clsph_particle;
+
+typedef struct {
+  uint32_t particles_count;
+  float max_velocity, fluid_density, total_mass, particle_mass, dynamic_viscosity,
+      simulation_time, target_fps, h, simulation_scale, time_delta, surface_tension_threshold,
+      surface_tension, restitution, K;
+  float padding_;
+  clsph_float3 constant_acceleration;
+  int32_t grid_size_x, grid_size_y, grid_size_z;
+  uint32_t grid_cell_count;
+  clsph_float3 min_point, max_point;
+} clsph_parameters;
+
+typedef struct {
+  float poly_6, poly_6_gradient, poly_6_laplacian, spiky, viscosity;
+} clsph_kernel_terms;
+
+typedef struct clsph_gpu clsph_gpu;
+
+/* Status codes. Values >= 256 are hard errors; the low bits are sticky
+ * device-side conditions reported by clsph_gpu_sync (they may be OR-ed). */
+enum {
+  CLSPH_OK = 0,
+  CLSPH_WARN_GRID_OVERFLOW = 1,  /* a grid axis reached 1024 cells: keys wrap
+                                    (the reference asserts, sph_simulation.cpp:301-303) */
+  CLSPH_WARN_COLLISION_CAP = 2,  /* an advect/collide loop hit its iteration cap
+                                    (the reference loop is unbounded, sph.cl:82-101) */
+  CLSPH_WARN_NONFINITE = 4,      /* a non-finite position was seen */
+  CLSPH_ERR_ARGUMENT = 256,
+  CLSPH_ERR_CUDA = 512,
+  CLSPH_ERR_NO_DEVICE = 1024,
+  CLSPH_ERR_STATE = 2048,        /* call out of order (e.g. step before upload) */
+  CLSPH_ERR_TOO_LARGE = 4096
+};
+
+/* Stages for clsph_gpu_step_until (parity inspection). */
+enum {
+  CLSPH_STAGE_GRID = 1,    /* bbox, grid parameters, keys */
+  CLSPH_STAGE_SORT = 2,    /* stable sort, gather, cell offsets */
+  CLSPH_STAGE_DENSITY = 3, /* density + pressure */
+  CLSPH_STAGE_FORCES = 4,  /* acceleration */
+  CLSPH_STAGE_ADVECT = 5   /* leapfrog + collision = full substep */
+};
+
+/* Replaces the context/queue/program/buffer set-up of sph_simulation::simulate
+ * (sph_simulation.cpp:400-434). Allocates all device memory for up to n
+ * particles on the current CUDA device; no allocation happens per substep.
+ * params: the derived parameter block of sph_simulation::load_settings
+ * (sph_simulation.cpp:459-559); particles_count is replaced by n. */
+int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
+                     clsph_gpu** out);
+int clsph_gpu_destroy(clsph_gpu* h);
+
+/* Launch stream (a cudaStream_t); NULL selects the handle's own stream. */
+int clsph_gpu_set_stream(clsph_gpu* h, void* cuda_stream);
+
+/* Replaces the per-substep mesh buffers of sph_simulation.cpp:350-373: the
+ * scene (scene.h:11-14 arrays) is uploaded once and indexed by a per-cell
+ * triangle list. Face order is kept, so hit selection equals the reference's
+ * brute-force loop (collisions.cl:21-87). */
+int clsph_gpu_set_mesh(clsph_gpu* h, const float* face_normals, const float* vertices,
+                       uint32_t vertex_count, const uint32_t* indices, uint32_t face_count);
+
+/* Replaces the enqueueWriteBuffer of sph_simulation.cpp:249-251: host AoS ->
+ * device. `particles` points to n clsph_particle (only position, velocity and
+ * intermediate_velocity are read, as in the reference). */
+int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles);
+
+/* Replaces the enqueueReadBuffer of sph_simulation.cpp:393-395: device -> host
+ * AoS in the current (sorted) order, with density, pressure and grid_index of
+ * the last substep and acceleration = 0, as the reference leaves them.
+ * Synchronises the stream. */
+int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles);
+
+/* `substeps` calls of simulate_single_frame (sph_simulation.cpp:227-398) with
+ * no host round trip in between. Asynchronous on the handle's stream. */
+int clsph_gpu_step(clsph_gpu* h, uint32_t substeps);
+
+/* One substep run up to and including `stage` (CLSPH_STAGE_*), for parity
+ * inspection with the read functions below. */
+int clsph_gpu_step_until(clsph_gpu* h, int stage);
+
+/* Waits for the stream; *flags (may be NULL) receives the sticky
+ * CLSPH_WARN_* bits accumulated since the last call, which are then cleared. */
+int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags);
+
+/* The parameter block with the grid of the last substep (min_point,
+ * max_point, grid_size_*, grid_cell_count), as sph_simulation keeps it. */
+int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out);
+
+/* Inspection (synchronising). keys: sorted grid_index per slot; perm: sorted
+ * slot -> slot before the sort (may be NULL). */
+int clsph_gpu_read_keys(clsph_gpu* h, uint32_t* keys, uint32_t* perm);
+
+/* The reference's dense cell table (sph_simulation.cpp:216-224) rebuilt from
+ * the device cell index: table[c] = first sorted slot with key >= c, for
+ * c < grid_cell_count. Needs cap >= grid_cell_count. Debug path: allocates. */
+int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap);
+
+/* density[n], pressure[n], accel[4n] (x, y, z, 0) of the last substep; any
+ * pointer may be NULL. accel is valid after CLSPH_STAGE_FORCES. */
+int clsph_gpu_read_fields(clsph_gpu* h, float* density, float* pressure, float* accel);
+
+/* Persistent particle ids per slot (identity at the first upload; they follow
+ * the particles through every sort). */
+int clsph_gpu_read_ids(clsph_gpu* h, uint32_t* ids);
+
+/* Per-kernel timing with CUDA events on the launch stream (0 = off). While
+ * on, clsph_gpu_kernel_times fills ms[i] with the summed duration of kernel
+ * class i and counts[i] with its launch count since the last reset. */
+int clsph_gpu_set_profiling(clsph_gpu* h, int enabled);
+int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_stride,
+                           float* ms, uint32_t* counts, int* n_classes);
+
+/* Counters since create: [0] substeps, [1] particles whose collision loop hit
+ * the cap, [2] kernel launches. */
+int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3);
+
+/* Text of the last error on this thread. */
+const char* clsph_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLSPH_GPU_H */

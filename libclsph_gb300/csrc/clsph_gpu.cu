@@ -1,0 +1,670 @@
+// C ABI of the GB300 SPH substep engine (include/clsph_gpu.h).
+//
+// One handle owns every device buffer for n particles (allocated once in
+// clsph_gpu_create), the scene mesh with its per-cell triangle lists, and a
+// stream. clsph_gpu_step enqueues the substep kernels of clsph_kernels.cuh;
+// no host round trip and no allocation happens between substeps.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "clsph_gpu.h"
+#include "clsph_kernels.cuh"
+
+using namespace clsph;
+
+static_assert(sizeof(clsph_particle) == 80, "particle layout");
+static_assert(sizeof(clsph_parameters) == 128, "parameter layout");
+static_assert(offsetof(clsph_parameters, constant_acceleration) == 64, "parameter layout");
+static_assert(offsetof(clsph_parameters, grid_size_x) == 80, "parameter layout");
+static_assert(offsetof(clsph_parameters, min_point) == 96, "parameter layout");
+static_assert(sizeof(clsph_kernel_terms) == 20, "kernel constant layout");
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+  do {                                                                                  \
+    cudaError_t err_ = (expr);                                                          \
+    if (err_ != cudaSuccess)                                                            \
+      return fail(CLSPH_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(err_)); \
+  } while (0)
+
+enum KernelClass {
+  K_GRID_SETUP,
+  K_KEYS,
+  K_RADIX_COUNT,
+  K_RADIX_SCAN,
+  K_RADIX_SCATTER,
+  K_GATHER,
+  K_DENSITY,
+  K_FORCES,
+  K_ADVECT,
+  K_UNPACK,
+  K_PACK,
+  K_MISC,
+  K_NUM_CLASSES
+};
+
+const char* kKernelNames[K_NUM_CLASSES] = {
+    "grid_setup", "keys", "radix_count", "radix_scan", "radix_scatter", "gather",
+    "density",    "forces", "advect",   "unpack_aos", "pack_aos",      "misc"};
+
+struct PendingTiming {
+  int cls;
+  cudaEvent_t start, stop;
+};
+
+template <typename T>
+int dev_alloc(T** p, size_t count) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+uint32_t grid_blocks(uint32_t n, uint32_t cap = 0) {
+  uint32_t b = (n + kBlock - 1) / kBlock;
+  if (b == 0) b = 1;
+  if (cap && b > cap) b = cap;
+  return b;
+}
+
+float pown_f(float x, int k) {
+  float r = x;
+  for (int i = 1; i < k; ++i) r = r * x;
+  return r;
+}
+
+}  // namespace
+
+struct clsph_gpu {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  uint32_t n = 0;
+  clsph_parameters params{};
+  clsph_kernel_terms terms{};
+  Consts consts{};
+
+  State st[2]{};
+  uint32_t* ids[2]{};
+  int ids_sel = 0;
+  float* rho = nullptr;
+  float* prs = nullptr;
+  float4* acc = nullptr;
+  uint32_t* keys = nullptr;  // [2n]
+  uint32_t* vals = nullptr;  // [2n]
+  uint32_t* tile_hist = nullptr;
+  uint32_t ntiles = 0;
+  uint32_t* digit_total = nullptr;
+  CellIndex ci{};
+  uint32_t slots = 0;
+  DevGrid* grid = nullptr;
+  uint32_t* bbox = nullptr;
+  uint32_t* status = nullptr;
+  unsigned long long* capped = nullptr;
+  float4* aos_stage = nullptr;
+
+  // mesh
+  float* d_normals = nullptr;
+  float* d_vertices = nullptr;
+  uint32_t* d_indices = nullptr;
+  uint32_t* d_cell_start = nullptr;
+  uint32_t* d_cell_faces = nullptr;
+  DevMesh mesh{};
+
+  bool uploaded = false;
+  bool partial = false;
+  bool have_fields = false;
+  uint32_t max_iters = 1024;
+
+  bool profiling = false;
+  std::vector<PendingTiming> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double class_ms[K_NUM_CLASSES] = {};
+  uint32_t class_count[K_NUM_CLASSES] = {};
+  uint64_t substeps = 0;
+  uint64_t launches = 0;
+
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+
+  template <typename Kernel, typename... Args>
+  void launch(int cls, Kernel k, dim3 g, dim3 b, Args... args) {
+    PendingTiming t{cls, nullptr, nullptr};
+    if (profiling) {
+      t.start = take_event();
+      cudaEventRecord(t.start, stream);
+    }
+    k<<<g, b, 0, stream>>>(args...);
+    ++launches;
+    if (profiling) {
+      t.stop = take_event();
+      cudaEventRecord(t.stop, stream);
+      pending.push_back(t);
+    }
+  }
+
+  void harvest() {
+    for (auto& t : pending) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, t.start, t.stop) == cudaSuccess) {
+        class_ms[t.cls] += ms;
+        class_count[t.cls] += 1;
+      }
+      event_pool.push_back(t.start);
+      event_pool.push_back(t.stop);
+    }
+    pending.clear();
+  }
+
+  void free_mesh() {
+    cudaFree(d_normals);
+    cudaFree(d_vertices);
+    cudaFree(d_indices);
+    cudaFree(d_cell_start);
+    cudaFree(d_cell_faces);
+    d_normals = d_vertices = nullptr;
+    d_indices = d_cell_start = d_cell_faces = nullptr;
+    mesh = DevMesh{};
+  }
+};
+
+namespace {
+
+void derive_consts(clsph_gpu* h) {
+  const clsph_parameters& p = h->params;
+  const clsph_kernel_terms& t = h->terms;
+  Consts& c = h->consts;
+  c.n = h->n;
+  c.h = p.h;
+  c.mass = p.particle_mass;
+  c.rho0 = p.fluid_density;
+  c.K = p.K;
+  c.mu = p.dynamic_viscosity;
+  c.sigma = p.surface_tension;
+  c.sigma_threshold = p.surface_tension_threshold;
+  c.restitution = p.restitution;
+  c.time_delta = p.time_delta;
+  c.scale = p.simulation_scale;
+  c.vmax = p.max_velocity;
+  c.gx = p.constant_acceleration.s[0];
+  c.gy = p.constant_acceleration.s[1];
+  c.gz = p.constant_acceleration.s[2];
+  c.poly6 = t.poly_6;
+  c.grad6 = t.poly_6_gradient;
+  c.lap6 = t.poly_6_laplacian;
+  c.spiky = t.spiky;
+  c.visc = t.viscosity;
+  // smoothing.cl:24: -45 / (float)(M_PI * pown(h, 6)) with M_PI in double
+  c.spiky_zero = -45.f / (float)(M_PI * (double)pown_f(p.h, 6));
+  c.cull_r2 = p.h * p.h * 1.0001f;
+}
+
+int enqueue_substep(clsph_gpu* h, int until) {
+  const uint32_t n = h->n;
+  const uint32_t blocks = grid_blocks(n);
+  h->launch(K_GRID_SETUP, k_grid_setup, dim3(1), dim3(256), h->bbox, h->grid, h->params.h,
+            h->status, h->digit_total);
+  CUDA_TRY(cudaMemsetAsync(h->ci.keys, 0, sizeof(uint32_t) * h->slots, h->stream));
+  h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n, h->grid,
+            h->keys);
+  if (until <= CLSPH_STAGE_GRID) return 0;
+  for (int pass = 0; pass < 4; ++pass) {
+    h->launch(K_RADIX_COUNT, k_radix_count, dim3(h->ntiles), dim3(kRadixThreads),
+              (const uint32_t*)h->keys, n, pass, (const DevGrid*)h->grid, h->tile_hist, h->ntiles,
+              h->digit_total);
+    h->launch(K_RADIX_SCAN, k_radix_scan, dim3(256), dim3(kRadixThreads), h->tile_hist, h->ntiles,
+              pass, (const DevGrid*)h->grid, (const uint32_t*)h->digit_total);
+    h->launch(K_RADIX_SCATTER, k_radix_scatter, dim3(h->ntiles), dim3(kRadixThreads), h->keys,
+              h->vals, n, pass, (const DevGrid*)h->grid, (const uint32_t*)h->tile_hist, h->ntiles);
+  }
+  const int src_ids = h->ids_sel, dst_ids = h->ids_sel ^ 1;
+  h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
+            (const uint32_t*)h->keys, (const uint32_t*)h->vals, h->st[0], h->st[1],
+            (const uint32_t*)h->ids[src_ids], h->ids[dst_ids], h->ci);
+  h->ids_sel = dst_ids;
+  if (until <= CLSPH_STAGE_SORT) return 0;
+  h->launch(K_DENSITY, k_density, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
+            (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci, h->consts, h->rho, h->prs);
+  if (until <= CLSPH_STAGE_DENSITY) return 0;
+  h->launch(K_FORCES, k_forces, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
+            (const uint32_t*)h->keys, h->st[1], (const float*)h->rho, (const float*)h->prs, h->ci,
+            h->consts, h->acc);
+  if (until <= CLSPH_STAGE_FORCES) return 0;
+  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, 152 * 8)), dim3(kBlock), n, h->st[1],
+            (const float4*)h->acc, h->st[0], h->mesh, h->consts, h->max_iters, h->bbox, h->status,
+            h->capped);
+  return 0;
+}
+
+int check_launch(clsph_gpu* h) {
+  (void)h;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int read_grid(clsph_gpu* h, DevGrid* g) {
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(g, h->grid, sizeof(DevGrid), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// Per-cell triangle lists over a uniform grid around the mesh. Every face
+// whose bounding box, grown by the list reach plus a tolerance, overlaps a
+// cell is listed there in ascending face order, so scanning one list equals
+// the reference's scan over all faces for any segment that starts in the
+// cell and is no longer than the reach.
+int build_face_grid(clsph_gpu* h, const float* vx, uint32_t nv, const uint32_t* ix, uint32_t faces,
+                    std::vector<uint32_t>& start, std::vector<uint32_t>& list) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t f = 0; f < faces; ++f)
+    for (int k = 0; k < 3; ++k) {
+      uint32_t v = ix[3 * f + k];
+      if (v >= nv) return fail(CLSPH_ERR_ARGUMENT, "mesh index out of range");
+      for (int a = 0; a < 3; ++a) {
+        float c = vx[3 * v + a];
+        if (!std::isfinite(c)) return 1;  // non-finite mesh: scan every face instead
+        lo[a] = std::fmin(lo[a], c);
+        hi[a] = std::fmax(hi[a], c);
+      }
+    }
+  const clsph_parameters& p = h->params;
+  float extent = 0.f;
+  for (int a = 0; a < 3; ++a) extent = std::fmax(extent, hi[a] - lo[a]);
+  const float reach = std::fmax(p.max_velocity * p.time_delta * p.simulation_scale * 1.5f + 0.002f, 1e-4f);
+  const float tol = 1e-4f * extent + 1e-5f;
+  const float pad = reach + tol;
+  float glo[3], ghi[3];
+  for (int a = 0; a < 3; ++a) {
+    glo[a] = lo[a] - pad;
+    ghi[a] = hi[a] + pad;
+  }
+  float cell = std::fmax((extent + 2 * pad) / 128.f, pad);
+  int dims[3];
+  for (;;) {
+    double total = 1.0;
+    for (int a = 0; a < 3; ++a) {
+      dims[a] = (int)std::ceil((ghi[a] - glo[a]) / cell);
+      if (dims[a] < 1) dims[a] = 1;
+      total *= dims[a];
+    }
+    if (total <= (double)(1u << 22)) break;
+    cell *= 1.25f;
+  }
+  const size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+  auto cell_range = [&](const float* mn, const float* mx, int* c0, int* c1) {
+    for (int a = 0; a < 3; ++a) {
+      int a0 = (int)std::floor((mn[a] - glo[a]) / cell);
+      int a1 = (int)std::floor((mx[a] - glo[a]) / cell);
+      c0[a] = a0 < 0 ? 0 : (a0 >= dims[a] ? dims[a] - 1 : a0);
+      c1[a] = a1 < 0 ? 0 : (a1 >= dims[a] ? dims[a] - 1 : a1);
+    }
+  };
+  std::vector<uint32_t> count(ncell + 1, 0u);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (uint32_t f = 0; f < faces; ++f) {
+      float mn[3], mx[3];
+      for (int a = 0; a < 3; ++a) {
+        float c0 = vx[3 * ix[3 * f] + a], c1 = vx[3 * ix[3 * f + 1] + a], c2 = vx[3 * ix[3 * f + 2] + a];
+        mn[a] = std::fmin(c0, std::fmin(c1, c2)) - pad - tol;
+        mx[a] = std::fmax(c0, std::fmax(c1, c2)) + pad + tol;
+      }
+      int c0[3], c1[3];
+      cell_range(mn, mx, c0, c1);
+      for (int z = c0[2]; z <= c1[2]; ++z)
+        for (int y = c0[1]; y <= c1[1]; ++y)
+          for (int x = c0[0]; x <= c1[0]; ++x) {
+            size_t c = ((size_t)z * dims[1] + y) * dims[0] + x;
+            if (pass == 0)
+              count[c]++;
+            else
+              list[start[c] + count[c]++] = f;
+          }
+    }
+    if (pass == 0) {
+      start.assign(ncell + 1, 0u);
+      uint64_t run = 0;
+      for (size_t c = 0; c < ncell; ++c) {
+        start[c] = (uint32_t)run;
+        run += count[c];
+        if (run > 0xFFFFFFFFull) return fail(CLSPH_ERR_TOO_LARGE, "face lists too large");
+      }
+      start[ncell] = (uint32_t)run;
+      list.assign(run ? run : 1, 0u);
+      std::fill(count.begin(), count.end(), 0u);
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    h->mesh.lo[a] = glo[a];
+    h->mesh.dims[a] = dims[a];
+  }
+  h->mesh.inv_cell = 1.f / cell;
+  h->mesh.reach = reach;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* clsph_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
+                     clsph_gpu** out) {
+  if (!params || !terms || !out || n == 0) return fail(CLSPH_ERR_ARGUMENT, "create: bad argument");
+  if (n > (1u << 28)) return fail(CLSPH_ERR_TOO_LARGE, "create: more than 2^28 particles");
+  if (!(params->h > 0.f)) return fail(CLSPH_ERR_ARGUMENT, "create: h must be positive");
+  int devices = 0;
+  if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
+    return fail(CLSPH_ERR_NO_DEVICE, "create: no CUDA device");
+  clsph_gpu* h = new clsph_gpu();
+  cudaGetDevice(&h->device);
+  h->n = n;
+  h->params = *params;
+  h->params.particles_count = n;
+  h->terms = *terms;
+  derive_consts(h);
+  int rc = 0;
+  auto bail = [&](int code) {
+    clsph_gpu_destroy(h);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "create: stream"));
+  h->stream = h->own_stream;
+  for (int s = 0; s < 2; ++s) {
+    if ((rc = dev_alloc(&h->st[s].pos, n)) || (rc = dev_alloc(&h->st[s].vel, n)) ||
+        (rc = dev_alloc(&h->st[s].ivel, n)) || (rc = dev_alloc(&h->ids[s], n)))
+      return bail(rc);
+  }
+  h->ntiles = (n + kRadixTile - 1) / kRadixTile;
+  uint32_t slots = 1024;
+  while (slots < 2u * n) slots <<= 1;
+  h->slots = slots;
+  uint32_t log2s = 0;
+  while ((1u << log2s) < slots) ++log2s;
+  if ((rc = dev_alloc(&h->rho, n)) || (rc = dev_alloc(&h->prs, n)) || (rc = dev_alloc(&h->acc, n)) ||
+      (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
+      (rc = dev_alloc(&h->tile_hist, 256 * (size_t)h->ntiles)) ||
+      (rc = dev_alloc(&h->digit_total, 4 * 256)) || (rc = dev_alloc(&h->ci.keys, slots)) ||
+      (rc = dev_alloc(&h->ci.start, slots)) || (rc = dev_alloc(&h->ci.end, slots)) ||
+      (rc = dev_alloc(&h->grid, 1)) || (rc = dev_alloc(&h->bbox, 6)) ||
+      (rc = dev_alloc(&h->status, 1)) || (rc = dev_alloc(&h->capped, 1)) ||
+      (rc = dev_alloc(&h->aos_stage, 5 * (size_t)n)))
+    return bail(rc);
+  h->ci.mask = slots - 1;
+  h->ci.shift = 32 - log2s;
+  if (cudaMemset(h->grid, 0, sizeof(DevGrid)) != cudaSuccess ||
+      cudaMemset(h->status, 0, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(h->capped, 0, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(h->rho, 0, sizeof(float) * n) != cudaSuccess ||
+      cudaMemset(h->prs, 0, sizeof(float) * n) != cudaSuccess ||
+      cudaMemset(h->acc, 0, sizeof(float4) * n) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "create: memset"));
+  // identity ids
+  std::vector<uint32_t> iota(n);
+  for (uint32_t i = 0; i < n; ++i) iota[i] = i;
+  if (cudaMemcpy(h->ids[0], iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "create: ids"));
+  *out = h;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_destroy(clsph_gpu* h) {
+  if (!h) return CLSPH_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& t : h->pending) {
+    cudaEventDestroy(t.start);
+    cudaEventDestroy(t.stop);
+  }
+  for (auto e : h->event_pool) cudaEventDestroy(e);
+  for (int s = 0; s < 2; ++s) {
+    cudaFree(h->st[s].pos);
+    cudaFree(h->st[s].vel);
+    cudaFree(h->st[s].ivel);
+    cudaFree(h->ids[s]);
+  }
+  cudaFree(h->rho);
+  cudaFree(h->prs);
+  cudaFree(h->acc);
+  cudaFree(h->keys);
+  cudaFree(h->vals);
+  cudaFree(h->tile_hist);
+  cudaFree(h->digit_total);
+  cudaFree(h->ci.keys);
+  cudaFree(h->ci.start);
+  cudaFree(h->ci.end);
+  cudaFree(h->grid);
+  cudaFree(h->bbox);
+  cudaFree(h->status);
+  cudaFree(h->capped);
+  cudaFree(h->aos_stage);
+  h->free_mesh();
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_stream(clsph_gpu* h, void* stream) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_stream: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_mesh(clsph_gpu* h, const float* normals, const float* vertices,
+                       uint32_t vertex_count, const uint32_t* indices, uint32_t faces) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_mesh: null handle");
+  if (faces && (!normals || !vertices || !indices))
+    return fail(CLSPH_ERR_ARGUMENT, "set_mesh: null mesh array");
+  for (uint64_t k = 0; k < 3ull * faces; ++k)
+    if (indices[k] >= vertex_count) return fail(CLSPH_ERR_ARGUMENT, "set_mesh: vertex index out of range");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->free_mesh();
+  if (faces == 0) return CLSPH_OK;
+  int rc;
+  if ((rc = dev_alloc(&h->d_normals, 3 * (size_t)faces)) ||
+      (rc = dev_alloc(&h->d_vertices, 3 * (size_t)vertex_count)) ||
+      (rc = dev_alloc(&h->d_indices, 3 * (size_t)faces)))
+    return rc;
+  CUDA_TRY(cudaMemcpy(h->d_normals, normals, sizeof(float) * 3 * faces, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->d_vertices, vertices, sizeof(float) * 3 * vertex_count, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->d_indices, indices, sizeof(uint32_t) * 3 * faces, cudaMemcpyHostToDevice));
+  h->mesh.normals = h->d_normals;
+  h->mesh.vertices = h->d_vertices;
+  h->mesh.indices = h->d_indices;
+  h->mesh.faces = faces;
+  std::vector<uint32_t> start, list;
+  rc = build_face_grid(h, vertices, vertex_count, indices, faces, start, list);
+  if (rc >= 256) return rc;
+  if (rc == 0) {
+    if ((rc = dev_alloc(&h->d_cell_start, start.size())) || (rc = dev_alloc(&h->d_cell_faces, list.size())))
+      return rc;
+    CUDA_TRY(cudaMemcpy(h->d_cell_start, start.data(), sizeof(uint32_t) * start.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_cell_faces, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice));
+    h->mesh.cell_start = h->d_cell_start;
+    h->mesh.cell_faces = h->d_cell_faces;
+  }
+  return CLSPH_OK;
+}
+
+int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles) {
+  if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "upload: bad argument");
+  CUDA_TRY(cudaMemcpyAsync(h->aos_stage, particles, sizeof(clsph_particle) * h->n,
+                           cudaMemcpyHostToDevice, h->stream));
+  h->launch(K_MISC, k_bbox_reset, dim3(1), dim3(32), h->bbox);
+  h->launch(K_UNPACK, k_unpack_aos, dim3(grid_blocks(h->n, 152 * 8)), dim3(kBlock),
+            (const float4*)h->aos_stage, h->n, h->st[0], h->bbox, h->status);
+  h->uploaded = true;
+  h->partial = false;
+  h->have_fields = false;
+  return check_launch(h);
+}
+
+int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles) {
+  if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "download: bad argument");
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "download: no complete state");
+  h->launch(K_PACK, k_pack_aos, dim3(grid_blocks(h->n, 152 * 8)), dim3(kBlock), h->aos_stage, h->n,
+            h->st[0], (const float*)h->rho, (const float*)h->prs, (const uint32_t*)h->keys,
+            (const DevGrid*)h->grid, h->have_fields ? 1 : 0);
+  CUDA_TRY(cudaMemcpyAsync(particles, h->aos_stage, sizeof(clsph_particle) * h->n,
+                           cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return check_launch(h);
+}
+
+int clsph_gpu_step(clsph_gpu* h, uint32_t substeps) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "step: null handle");
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step: upload particles first");
+  for (uint32_t s = 0; s < substeps; ++s) {
+    int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+    if (rc) return rc;
+    ++h->substeps;
+  }
+  if (substeps) h->have_fields = true;
+  return check_launch(h);
+}
+
+int clsph_gpu_step_until(clsph_gpu* h, int stage) {
+  if (!h || stage < CLSPH_STAGE_GRID || stage > CLSPH_STAGE_ADVECT)
+    return fail(CLSPH_ERR_ARGUMENT, "step_until: bad argument");
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step_until: upload particles first");
+  int rc = enqueue_substep(h, stage);
+  if (rc) return rc;
+  ++h->substeps;
+  if (stage < CLSPH_STAGE_ADVECT) h->partial = true;
+  h->have_fields = stage >= CLSPH_STAGE_DENSITY;
+  return check_launch(h);
+}
+
+int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "sync: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  uint32_t f = 0;
+  CUDA_TRY(cudaMemcpy(&f, h->status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemset(h->status, 0, sizeof(uint32_t)));
+  if (flags) *flags = f;
+  if (h->profiling) h->harvest();
+  return CLSPH_OK;
+}
+
+int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out) {
+  if (!h || !out) return fail(CLSPH_ERR_ARGUMENT, "get_parameters: bad argument");
+  DevGrid g;
+  int rc = read_grid(h, &g);
+  if (rc) return rc;
+  *out = h->params;
+  for (int a = 0; a < 3; ++a) {
+    out->min_point.s[a] = g.lo[a];
+    out->max_point.s[a] = g.hi[a];
+  }
+  out->min_point.s[3] = out->max_point.s[3] = 0.f;
+  out->grid_size_x = g.size[0];
+  out->grid_size_y = g.size[1];
+  out->grid_size_z = g.size[2];
+  out->grid_cell_count = g.cells;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_read_keys(clsph_gpu* h, uint32_t* keys, uint32_t* perm) {
+  if (!h || !keys) return fail(CLSPH_ERR_ARGUMENT, "read_keys: bad argument");
+  DevGrid g;
+  int rc = read_grid(h, &g);
+  if (rc) return rc;
+  const size_t off = (size_t)sorted_sel(g) * h->n;
+  CUDA_TRY(cudaMemcpy(keys, h->keys + off, sizeof(uint32_t) * h->n, cudaMemcpyDeviceToHost));
+  if (perm) CUDA_TRY(cudaMemcpy(perm, h->vals + off, sizeof(uint32_t) * h->n, cudaMemcpyDeviceToHost));
+  return CLSPH_OK;
+}
+
+int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap) {
+  if (!h || !table) return fail(CLSPH_ERR_ARGUMENT, "read_cell_table: bad argument");
+  DevGrid g;
+  int rc = read_grid(h, &g);
+  if (rc) return rc;
+  if (cap < g.cells) return fail(CLSPH_ERR_ARGUMENT, "read_cell_table: buffer too small");
+  if (g.cells == 0) return CLSPH_OK;
+  uint32_t* d = nullptr;
+  if ((rc = dev_alloc(&d, g.cells))) return rc;
+  k_dense_table<<<(g.cells + 255) / 256, 256, 0, h->stream>>>(h->keys, h->n, h->grid, d);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(table, d, sizeof(uint32_t) * g.cells, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("read_cell_table: ") + cudaGetErrorString(e));
+  return CLSPH_OK;
+}
+
+int clsph_gpu_read_fields(clsph_gpu* h, float* density, float* pressure, float* accel) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "read_fields: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (density) CUDA_TRY(cudaMemcpy(density, h->rho, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
+  if (pressure) CUDA_TRY(cudaMemcpy(pressure, h->prs, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
+  if (accel) CUDA_TRY(cudaMemcpy(accel, h->acc, sizeof(float4) * h->n, cudaMemcpyDeviceToHost));
+  return CLSPH_OK;
+}
+
+int clsph_gpu_read_ids(clsph_gpu* h, uint32_t* ids) {
+  if (!h || !ids) return fail(CLSPH_ERR_ARGUMENT, "read_ids: bad argument");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(ids, h->ids[h->ids_sel], sizeof(uint32_t) * h->n, cudaMemcpyDeviceToHost));
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_profiling(clsph_gpu* h, int enabled) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_profiling: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->harvest();
+  h->profiling = enabled != 0;
+  for (int k = 0; k < K_NUM_CLASSES; ++k) {
+    h->class_ms[k] = 0.0;
+    h->class_count[k] = 0;
+  }
+  return CLSPH_OK;
+}
+
+int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_stride, float* ms,
+                           uint32_t* counts, int* n_classes) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "kernel_times: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->harvest();
+  int k_out = max_classes < K_NUM_CLASSES ? max_classes : K_NUM_CLASSES;
+  for (int k = 0; k < k_out; ++k) {
+    if (names && name_stride > 0) std::snprintf(names + (size_t)k * name_stride, name_stride, "%s", kKernelNames[k]);
+    if (ms) ms[k] = (float)h->class_ms[k];
+    if (counts) counts[k] = h->class_count[k];
+  }
+  if (n_classes) *n_classes = K_NUM_CLASSES;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3) {
+  if (!h || !out3) return fail(CLSPH_ERR_ARGUMENT, "counters: bad argument");
+  unsigned long long capped = 0;
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(&capped, h->capped, sizeof(capped), cudaMemcpyDeviceToHost));
+  out3[0] = h->substeps;
+  out3[1] = capped;
+  out3[2] = h->launches;
+  return CLSPH_OK;
+}
+
+}  // extern "C"

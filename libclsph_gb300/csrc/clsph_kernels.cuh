@@ -1,0 +1,699 @@
+// Device kernels of one SPH substep (sm_103a).
+//
+// Data layout in HBM (SoA, sorted order, 16-byte float4 rows):
+//   pos[n], vel[n], ivel[n]   position, velocity, intermediate (half-step) velocity
+//   rho[n], prs[n]            density and Tait pressure of the substep
+//   acc[n]                    acceleration (forces -> advection)
+//   keys[2][n], vals[2][n]    radix-sort ping-pong (Morton key, source slot)
+//   ids[2][n]                 persistent particle ids (the reference has none)
+//   hkeys[S], hstart[S], hend[S]  cell index: Morton key -> [start, end)
+// The per-substep grid (bounding box, cell size, dense cell count, number
+// of radix passes) lives in device memory (DevGrid) so that no host round
+// trip is needed between kernels.
+#pragma once
+
+#include "clsph_common.cuh"
+
+namespace clsph {
+
+constexpr int kBlock = 256;
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 16;
+constexpr int kRadixTile = kRadixThreads * kRadixItems;  // 4096 keys per tile
+constexpr int kRadixWarps = kRadixThreads / 32;
+constexpr int kRadixWarpSpan = kRadixTile / kRadixWarps;  // 512 keys per warp
+
+enum : uint32_t {
+  kFlagGridOverflow = 1u,
+  kFlagCollisionCap = 2u,
+  kFlagNonFinite = 4u,
+};
+
+struct DevGrid {
+  float lo[3];
+  float hi[3];
+  float cell;           // 2h
+  int32_t size[3];      // grid_size_x/y/z
+  uint32_t cells;       // grid_cell_count (dense Morton range)
+  uint32_t maxkey;      // largest key of the substep (sets the radix passes)
+  uint32_t pad_[4];
+};
+
+// 8-bit radix passes that cover every key of the substep.
+__host__ __device__ __forceinline__ uint32_t radix_passes(const DevGrid& g) {
+  uint32_t k = g.maxkey | 1u, bits = 0;
+  while (k) { ++bits; k >>= 1; }
+  return (bits + 7u) / 8u;
+}
+// Ping-pong buffer that holds the sorted keys and slots after all passes.
+__host__ __device__ __forceinline__ uint32_t sorted_sel(const DevGrid& g) {
+  return radix_passes(g) & 1u;
+}
+
+// Per-substep constants (kernel argument).
+struct Consts {
+  uint32_t n;
+  float h, mass, rho0, K, mu, sigma, sigma_threshold, restitution;
+  float time_delta, scale, vmax;
+  float gx, gy, gz;
+  float poly6, grad6, lap6, spiky, visc, spiky_zero;
+  float cull_r2;  // conservative h^2 for the FMA cull test
+};
+
+struct State {
+  float4* pos;
+  float4* vel;
+  float4* ivel;
+};
+
+struct CellIndex {
+  uint32_t* keys;   // key + 1, 0 = empty
+  uint32_t* start;
+  uint32_t* end;
+  uint32_t mask;    // slots - 1 (power of two)
+  uint32_t shift;   // 32 - log2(slots)
+};
+
+struct DevMesh {
+  const float* normals;     // 3 per face
+  const float* vertices;    // 3 per vertex
+  const uint32_t* indices;  // 3 per face
+  uint32_t faces;
+  // per-cell triangle lists (CSR over a uniform grid covering the mesh)
+  const uint32_t* cell_start;  // dims product + 1
+  const uint32_t* cell_faces;
+  float lo[3];
+  float inv_cell;
+  int32_t dims[3];
+  float reach;  // longest segment a cell list covers
+};
+
+// ------------------------------------------------------------ cell index
+__device__ __forceinline__ uint32_t cell_slot_insert(const CellIndex& ci, uint32_t key) {
+  const uint32_t tag = key + 1u;
+  uint32_t slot = cell_hash(key) >> ci.shift;
+  for (uint32_t probe = 0; probe <= ci.mask; ++probe) {
+    uint32_t prev = atomicCAS(&ci.keys[slot], 0u, tag);
+    if (prev == 0u || prev == tag) return slot;
+    slot = (slot + 1u) & ci.mask;
+  }
+  return 0xFFFFFFFFu;  // unreachable: at most n keys in >= 2n slots
+}
+
+__device__ __forceinline__ uint2 cell_lookup(const CellIndex& ci, uint32_t key) {
+  const uint32_t tag = key + 1u;
+  uint32_t slot = cell_hash(key) >> ci.shift;
+  for (uint32_t probe = 0; probe <= ci.mask; ++probe) {
+    uint32_t k = __ldg(&ci.keys[slot]);
+    if (k == tag) return make_uint2(__ldg(&ci.start[slot]), __ldg(&ci.end[slot]));
+    if (k == 0u) break;
+    slot = (slot + 1u) & ci.mask;
+  }
+  return make_uint2(0u, 0u);
+}
+
+// ---------------------------------------------------- neighbour cell window
+// The support radius is h but cells are 2h wide (grid.cl:56-61 vs
+// smoothing.cl:2), so along each axis only the neighbour cell on the side of
+// the particle's half of its own cell can hold particles within h. Cells
+// outside that window contribute exact zeros in the reference, so skipping
+// them keeps the reference's summation sequence. Particles within 1/256 of a
+// cell's middle keep all three cells (margin >> float rounding of t).
+struct Window {
+  uint32_t lo[3], hi[3];
+};
+
+__device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const DevGrid& g) {
+  const uint32_t c[3] = {compact_bits3(key), compact_bits3(key >> 1), compact_bits3(key >> 2)};
+  const float pc[3] = {p.x, p.y, p.z};
+  Window w;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float t = XDIV(XSUB(pc[a], g.lo[a]), g.cell);
+    float frac = t - (float)c[a];
+    const float eps = 1.0f / 256.0f;
+    w.lo[a] = (frac < 0.5f + eps) ? c[a] - 1u : c[a];
+    w.hi[a] = (frac > 0.5f - eps) ? c[a] + 1u : c[a];
+  }
+  return w;
+}
+
+// --------------------------------------------------------------- kernels
+
+// Single-thread grid set-up (sph_simulation.cpp:253-306) from the bounding
+// box accumulated by the previous kernel; resets the box and the radix digit
+// totals for this substep.
+__global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ grid, float h,
+                             uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total) {
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) digit_total[i] = 0u;
+  if (threadIdx.x != 0) return;
+  const float cell = XMUL(h, 2.f);
+  DevGrid g;
+  bool overflow = false;
+  for (int a = 0; a < 3; ++a) {
+    float mn = ord2f(bbox[a]);
+    float mx = ord2f(bbox[3 + a]);
+    mn = XSUB(mn, XMUL(cell, 2.f));
+    mx = XADD(mx, XMUL(cell, 2.f));
+    g.lo[a] = mn;
+    g.hi[a] = mx;
+    uint32_t sz = __float2uint_rz(XDIV(XSUB(mx, mn), cell));
+    g.size[a] = (int32_t)sz;
+    if (g.size[a] < 0 || g.size[a] >= 1024) overflow = true;
+  }
+  g.cell = cell;
+  g.cells = morton3((uint32_t)g.size[0], (uint32_t)g.size[1], (uint32_t)g.size[2]);
+  g.maxkey = 0u;
+  for (int i = 0; i < 4; ++i) g.pad_[i] = 0u;
+  *grid = g;
+  if (overflow) atomicOr(status, kFlagGridOverflow);
+  // sentinels of sph_simulation.cpp:258-259 for the next accumulation
+  for (int a = 0; a < 3; ++a) {
+    bbox[a] = f2ord(2147483648.0f);
+    bbox[3 + a] = f2ord(-2147483648.0f);
+  }
+}
+
+__global__ void k_bbox_reset(uint32_t* __restrict__ bbox) {
+  if (threadIdx.x < 3) {
+    bbox[threadIdx.x] = f2ord(2147483648.0f);
+    bbox[3 + threadIdx.x] = f2ord(-2147483648.0f);
+  }
+}
+
+// Block-level min/max of positions, then one atomic per block and axis.
+// NaN coordinates are ignored, as the reference's `<` / `>` tests do.
+__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, uint32_t* bbox) {
+  __shared__ float red[6][kBlock / 32];
+  float v[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      float o = __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+      v[k] = k < 3 ? fminf(v[k], o) : fmaxf(v[k], o);
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      float x = lane < nw ? red[k][lane] : __int_as_float(0x7FC00000);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        float o = __shfl_xor_sync(0xFFFFFFFFu, x, off);
+        x = k < 3 ? fminf(x, o) : fmaxf(x, o);
+      }
+      if (lane == 0 && x == x) {
+        if (k < 3)
+          atomicMin(&bbox[k], f2ord(x));
+        else
+          atomicMax(&bbox[k], f2ord(x));
+      }
+    }
+  }
+}
+
+// Host AoS (80-byte particle) -> SoA state, with bounding box.
+__global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State st,
+                             uint32_t* __restrict__ bbox, uint32_t* __restrict__ status) {
+  const float qnan = __int_as_float(0x7FC00000);
+  float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4* p = aos + (size_t)i * 5;
+    float4 pos = p[0], vel = p[1], ivel = p[2];
+    pos.w = 0.f;
+    vel.w = 0.f;
+    ivel.w = 0.f;
+    st.pos[i] = pos;
+    st.vel[i] = vel;
+    st.ivel[i] = ivel;
+    lo = make_float3(fminf(lo.x, pos.x), fminf(lo.y, pos.y), fminf(lo.z, pos.z));
+    hi = make_float3(fmaxf(hi.x, pos.x), fmaxf(hi.y, pos.y), fmaxf(hi.z, pos.z));
+    if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
+  }
+  bbox_accumulate(lo, hi, bbox);
+}
+
+// SoA -> host AoS: acceleration is 0 after the advection loop (sph.cl:97-99).
+__global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
+                           const float* __restrict__ rho, const float* __restrict__ prs,
+                           const uint32_t* __restrict__ keys_base, const DevGrid* __restrict__ grid,
+                           int have_fields) {
+  const uint32_t sel = have_fields ? sorted_sel(*grid) : 0u;
+  const uint32_t* keys = keys_base + (size_t)sel * n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4* p = aos + (size_t)i * 5;
+    p[0] = st.pos[i];
+    p[1] = st.vel[i];
+    p[2] = st.ivel[i];
+    p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 tail;
+    tail.x = have_fields ? rho[i] : 0.f;
+    tail.y = have_fields ? prs[i] : 0.f;
+    tail.z = __uint_as_float(have_fields ? keys[i] : 0u);
+    tail.w = 0.f;
+    p[4] = tail;
+  }
+}
+
+// Morton key per particle (grid.cl:56-66) and the largest key.
+__global__ void __launch_bounds__(kBlock)
+    k_keys(const float4* __restrict__ pos, uint32_t n, DevGrid* __restrict__ grid,
+           uint32_t* __restrict__ keys) {
+  __shared__ uint32_t block_max;
+  if (threadIdx.x == 0) block_max = 0u;
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t key = 0u;
+  if (i < n) {
+    const DevGrid& g = *grid;
+    const float4 p = pos[i];
+    uint32_t cx = __float2uint_rz(XDIV(XSUB(p.x, g.lo[0]), g.cell));
+    uint32_t cy = __float2uint_rz(XDIV(XSUB(p.y, g.lo[1]), g.cell));
+    uint32_t cz = __float2uint_rz(XDIV(XSUB(p.z, g.lo[2]), g.cell));
+    key = morton3(cx, cy, cz);
+    keys[i] = key;
+  }
+  key = __reduce_max_sync(0xFFFFFFFFu, key);
+  if ((threadIdx.x & 31) == 0) atomicMax(&block_max, key);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(&grid->maxkey, block_max);
+}
+
+// ---------------------------------------------------------------- radix sort
+// Stable LSD radix sort of (key, slot) with 8-bit digits: count -> scan ->
+// scatter per pass. Passes beyond DevGrid::passes return at once, so the
+// launch sequence is fixed (graph-capturable) while the work follows the
+// key width. Ping-pong: pass p reads buffer p&1 and writes (p+1)&1.
+__global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
+                              const DevGrid* __restrict__ grid, uint32_t* __restrict__ tile_hist,
+                              uint32_t ntiles, uint32_t* __restrict__ digit_total) {
+  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  __shared__ uint32_t hist[256];
+  hist[threadIdx.x] = 0u;
+  __syncthreads();
+  const uint32_t* keys = keys_base + (size_t)(pass & 1) * n;
+  const uint32_t base = blockIdx.x * kRadixTile;
+  const int shift = 8 * pass;
+#pragma unroll 4
+  for (int k = 0; k < kRadixItems; ++k) {
+    uint32_t idx = base + k * kRadixThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&hist[(__ldg(&keys[idx]) >> shift) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  uint32_t c = hist[threadIdx.x];
+  tile_hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
+  if (c) atomicAdd(&digit_total[pass * 256 + threadIdx.x], c);
+}
+
+// One block per digit: exclusive scan of that digit's per-tile counts plus
+// the number of keys with a smaller digit.
+__global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, int pass,
+                             const DevGrid* __restrict__ grid,
+                             const uint32_t* __restrict__ digit_total) {
+  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  __shared__ uint32_t warp_sums[kRadixThreads / 32];
+  __shared__ uint32_t base_s;
+  const uint32_t d = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // base = sum of totals of smaller digits
+  uint32_t part = threadIdx.x < d ? digit_total[pass * 256 + threadIdx.x] : 0u;
+  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, off);
+  if (lane == 0) warp_sums[warp] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t b = 0;
+    for (int w = 0; w < kRadixThreads / 32; ++w) b += warp_sums[w];
+    base_s = b;
+  }
+  __syncthreads();
+  uint32_t carry = base_s;
+  uint32_t* row = tile_hist + (size_t)d * ntiles;
+  for (uint32_t chunk = 0; chunk < ntiles; chunk += kRadixThreads) {
+    uint32_t idx = chunk + threadIdx.x;
+    uint32_t v = idx < ntiles ? row[idx] : 0u;
+    uint32_t x = v;  // inclusive warp scan
+    for (int off = 1; off < 32; off <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+      if (lane >= off) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    uint32_t wbase = 0, total = 0;
+    for (int w = 0; w < kRadixThreads / 32; ++w) {
+      uint32_t s = warp_sums[w];
+      if (w < warp) wbase += s;
+      total += s;
+    }
+    if (idx < ntiles) row[idx] = carry + wbase + x - v;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kRadixThreads)
+    k_radix_scatter(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
+                    int pass, const DevGrid* __restrict__ grid,
+                    const uint32_t* __restrict__ tile_hist, uint32_t ntiles) {
+  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  __shared__ uint32_t cnt[kRadixWarps][256];
+  __shared__ uint32_t tile_off[256];
+  const uint32_t* keys_in = keys_base + (size_t)(pass & 1) * n;
+  uint32_t* keys_out = keys_base + (size_t)((pass + 1) & 1) * n;
+  const uint32_t* vals_in = vals_base + (size_t)(pass & 1) * n;
+  uint32_t* vals_out = vals_base + (size_t)((pass + 1) & 1) * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = 0; w < kRadixWarps; ++w) cnt[w][threadIdx.x] = 0u;
+  tile_off[threadIdx.x] = tile_hist[(size_t)threadIdx.x * ntiles + blockIdx.x];
+  __syncthreads();
+  const int shift = 8 * pass;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t base = blockIdx.x * kRadixTile + warp * kRadixWarpSpan;
+  uint32_t key[kRadixItems], val[kRadixItems], rank[kRadixItems];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const uint32_t idx = base + r * 32 + lane;
+    const bool valid = idx < n;
+    key[r] = valid ? keys_in[idx] : 0u;
+    val[r] = valid ? (pass == 0 ? idx : vals_in[idx]) : 0u;
+    const uint32_t d = valid ? ((key[r] >> shift) & 0xFFu) : 256u;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    uint32_t rk = 0;
+    if (valid) rk = cnt[warp][d] + __popc(peers & lt_mask);
+    __syncwarp();
+    if (valid && (peers & lt_mask) == 0u) cnt[warp][d] += __popc(peers);
+    __syncwarp();
+    rank[r] = valid ? ((rk << 8) | d) : 0xFFFFFFFFu;
+  }
+  __syncthreads();
+  {  // exclusive prefix over warps, per digit
+    uint32_t run = 0;
+    for (int w = 0; w < kRadixWarps; ++w) {
+      uint32_t t = cnt[w][threadIdx.x];
+      cnt[w][threadIdx.x] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    if (rank[r] == 0xFFFFFFFFu) continue;
+    const uint32_t d = rank[r] & 0xFFu;
+    const uint32_t dst = tile_off[d] + cnt[warp][d] + (rank[r] >> 8);
+    keys_out[dst] = key[r];
+    vals_out[dst] = val[r];
+  }
+}
+
+// Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
+// and records every cell's [start, end) in the cell index (the dense cell
+// table of sph_simulation.cpp:216-224 in compact form).
+__global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grid,
+                         const uint32_t* __restrict__ keys_base,
+                         const uint32_t* __restrict__ vals_base, State src, State dst,
+                         const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
+                         CellIndex ci) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t sel = sorted_sel(*grid);
+  const uint32_t* keys = keys_base + (size_t)sel * n;
+  const uint32_t* perm = vals_base + (size_t)sel * n;
+  const uint32_t from = perm[s];
+  dst.pos[s] = src.pos[from];
+  dst.vel[s] = src.vel[from];
+  dst.ivel[s] = src.ivel[from];
+  ids_dst[s] = ids_src[from];
+  const uint32_t key = keys[s];
+  if (s == 0 || keys[s - 1] != key) {
+    uint32_t slot = cell_slot_insert(ci, key);
+    if (slot != 0xFFFFFFFFu) ci.start[slot] = s;
+  }
+  if (s + 1 == n || keys[s + 1] != key) {
+    uint32_t slot = cell_slot_insert(ci, key);
+    if (slot != 0xFFFFFFFFu) ci.end[slot] = s + 1;
+  }
+}
+
+// Density (forces.cl:15-43) and Tait pressure (sph.cl:36-39).
+__global__ void __launch_bounds__(kBlock)
+    k_density(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
+              const float4* __restrict__ pos, CellIndex ci, Consts c, float* __restrict__ rho_out,
+              float* __restrict__ prs_out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DevGrid g = *grid;
+  const uint32_t* keys = keys_base + (size_t)(sorted_sel(g)) * n;
+  const float4 pi = pos[i];
+  const Window w = neighbour_window(pi, keys[i], g);
+  const float hh = XMUL(c.h, c.h);
+  float rho = 0.f;
+  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
+    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
+      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
+        const uint2 r = cell_lookup(ci, morton3(x, y, z));
+        for (uint32_t j = r.x; j < r.y; ++j) {
+          const float4 pj = __ldg(&pos[j]);
+          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          if (r2 > c.cull_r2) continue;
+          const float rr = xnorm(d);
+          if (!(XDIV(rr, c.h) < 1.f)) continue;  // outside support: exact zero
+          const float q = XSUB(hh, XMUL(rr, rr));
+          rho = XADD(rho, XMUL(c.mass, XMUL(c.poly6, XMUL(XMUL(q, q), q))));
+        }
+      }
+  rho_out[i] = rho;
+  const float x = XDIV(rho, c.rho0);
+  float p7 = x;
+#pragma unroll
+  for (int k = 1; k < 7; ++k) p7 = XMUL(p7, x);
+  prs_out[i] = XMUL(c.K, XSUB(p7, 1.f));
+}
+
+// Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58).
+__global__ void __launch_bounds__(kBlock)
+    k_forces(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
+             State st, const float* __restrict__ rho, const float* __restrict__ prs, CellIndex ci,
+             Consts c, float4* __restrict__ acc_out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DevGrid g = *grid;
+  const uint32_t* keys = keys_base + (size_t)(sorted_sel(g)) * n;
+  const float4 pi = st.pos[i];
+  const float4 vi = st.vel[i];
+  const float rho_i = rho[i];
+  const float own = XDIV(prs[i], XMUL(rho_i, rho_i));
+  const Window w = neighbour_window(pi, keys[i], g);
+  const float hh = XMUL(c.h, c.h);
+  const float lap_b = XMUL(3.f, hh);
+  V3 P = {0.f, 0.f, 0.f}, Vs = {0.f, 0.f, 0.f}, Nm = {0.f, 0.f, 0.f};
+  float lap = 0.f;
+  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
+    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
+      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
+        const uint2 r = cell_lookup(ci, morton3(x, y, z));
+        for (uint32_t j = r.x; j < r.y; ++j) {
+          const float4 pj = __ldg(&st.pos[j]);
+          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+          if (r2 > c.cull_r2) continue;
+          const float rr = xnorm(d);
+          if (!(XDIV(rr, c.h) < 1.f)) continue;  // every term is an exact zero
+          const float rho_j = __ldg(&rho[j]);
+          const float mj = XDIV(c.mass, rho_j);
+          if (j != i) {
+            const float coef = XMUL(XADD(XDIV(__ldg(&prs[j]), XMUL(rho_j, rho_j)), own), c.mass);
+            V3 sg;
+            if (XSUB(rr, 0.0000001f) < 0.f) {  // smoothing.cl:23-25
+              sg = {c.spiky_zero, c.spiky_zero, c.spiky_zero};
+            } else {
+              const float q = XSUB(c.h, rr);
+              const float q2 = XMUL(q, q);
+              sg = {XMUL(XMUL(c.spiky, XDIV(d.x, rr)), q2), XMUL(XMUL(c.spiky, XDIV(d.y, rr)), q2),
+                    XMUL(XMUL(c.spiky, XDIV(d.z, rr)), q2)};
+            }
+            P.x = XADD(P.x, XMUL(coef, sg.x));
+            P.y = XADD(P.y, XMUL(coef, sg.y));
+            P.z = XADD(P.z, XMUL(coef, sg.z));
+            const float vl = XMUL(c.visc, XSUB(c.h, rr));
+            const float4 vj = __ldg(&st.vel[j]);
+            Vs.x = XADD(Vs.x, XMUL(XMUL(XSUB(vj.x, vi.x), mj), vl));
+            Vs.y = XADD(Vs.y, XMUL(XMUL(XSUB(vj.y, vi.y), mj), vl));
+            Vs.z = XADD(Vs.z, XMUL(XMUL(XSUB(vj.z, vi.z), mj), vl));
+          }
+          const float q = XSUB(hh, XMUL(rr, rr));
+          const float q2 = XMUL(q, q);
+          Nm.x = XADD(Nm.x, XMUL(mj, XMUL(XMUL(c.grad6, d.x), q2)));
+          Nm.y = XADD(Nm.y, XMUL(mj, XMUL(XMUL(c.grad6, d.y), q2)));
+          Nm.z = XADD(Nm.z, XMUL(mj, XMUL(XMUL(c.grad6, d.z), q2)));
+          lap = XADD(lap, XMUL(mj, XMUL(XMUL(c.lap6, q), XSUB(lap_b, XMUL(7.f, XMUL(rr, rr))))));
+        }
+      }
+  const float nr = -rho_i;
+  V3 sum = {XADD(XMUL(nr, P.x), XMUL(Vs.x, c.mu)), XADD(XMUL(nr, P.y), XMUL(Vs.y, c.mu)),
+            XADD(XMUL(nr, P.z), XMUL(Vs.z, c.mu))};
+  const float nl = xnorm(Nm);
+  if (nl > c.sigma_threshold) {
+    const float s = XMUL(-c.sigma, lap);
+    sum.x = XADD(sum.x, XDIV(XMUL(s, Nm.x), nl));
+    sum.y = XADD(sum.y, XDIV(XMUL(s, Nm.y), nl));
+    sum.z = XADD(sum.z, XDIV(XMUL(s, Nm.z), nl));
+  }
+  acc_out[i] = make_float4(XADD(XDIV(sum.x, rho_i), c.gx), XADD(XDIV(sum.y, rho_i), c.gy),
+                           XADD(XDIV(sum.z, rho_i), c.gz), 0.f);
+}
+
+// ------------------------------------------------------- mesh collision
+struct Hit {
+  V3 point, normal;
+  float depth;
+  bool any;
+};
+
+// One face of collisions.cl:21-87 (nearest hit; an equal distance replaces).
+__device__ __forceinline__ void test_face(const DevMesh& m, uint32_t f, V3 p0, V3 p1, V3 d,
+                                          float dlen, Hit& h) {
+  V3 nrm = {__ldg(&m.normals[3 * f]), __ldg(&m.normals[3 * f + 1]), __ldg(&m.normals[3 * f + 2])};
+  if (XDIV(xdot(nrm, d), XMUL(xnorm(nrm), dlen)) <= 0.f) nrm = {-nrm.x, -nrm.y, -nrm.z};
+  const uint32_t ia = __ldg(&m.indices[3 * f]), ib = __ldg(&m.indices[3 * f + 1]),
+                 ic = __ldg(&m.indices[3 * f + 2]);
+  const V3 v0 = {__ldg(&m.vertices[3 * ia]), __ldg(&m.vertices[3 * ia + 1]), __ldg(&m.vertices[3 * ia + 2])};
+  const V3 v1 = {__ldg(&m.vertices[3 * ib]), __ldg(&m.vertices[3 * ib + 1]), __ldg(&m.vertices[3 * ib + 2])};
+  const V3 v2 = {__ldg(&m.vertices[3 * ic]), __ldg(&m.vertices[3 * ic + 1]), __ldg(&m.vertices[3 * ic + 2])};
+  const V3 u = xsub3(v1, v0), v = xsub3(v2, v0);
+  const float den = xdot(nrm, d);
+  if (den == 0.f) return;
+  const float r = XDIV(xdot(nrm, xsub3(v0, p0)), den);
+  if (!(0.f <= r && r <= 1.f)) return;
+  const V3 at = {XADD(p0.x, XMUL(r, d.x)), XADD(p0.y, XMUL(r, d.y)), XADD(p0.z, XMUL(r, d.z))};
+  const V3 w = xsub3(at, v0);
+  const float uv = xdot(u, v), wv = xdot(w, v), vv = xdot(v, v), wu = xdot(w, u), uu = xdot(u, u);
+  const float den2 = XSUB(XMUL(uv, uv), XMUL(uu, vv));
+  const float s = XDIV(XSUB(XMUL(uv, wv), XMUL(vv, wu)), den2);
+  const float t = XDIV(XSUB(XMUL(uv, wu), XMUL(uu, wv)), den2);
+  if (s >= 0.f && t >= 0.f && XADD(s, t) <= 1.f) {
+    if (h.any && xnorm(xsub3(p0, at)) > xnorm(xsub3(p0, h.point))) return;
+    h.normal = nrm;
+    h.point = at;
+    h.depth = xnorm(xsub3(p1, at));
+    h.any = true;
+  }
+}
+
+// Faces that can meet the segment, in ascending face order: the list of
+// the cell holding p0 when the segment is short enough for that list, no
+// face when p0 lies outside the list grid (nothing within reach), else all.
+__device__ __forceinline__ bool nearest_hit(const DevMesh& m, V3 p0, V3 p1, Hit& h) {
+  h.any = false;
+  if (m.faces == 0) return false;
+  const V3 d = xsub3(p1, p0);
+  const float dlen = xnorm(d);
+  uint32_t first = 0, last = m.faces;
+  const uint32_t* list = nullptr;
+  if (m.cell_start != nullptr && dlen <= m.reach) {
+    const float t[3] = {(p0.x - m.lo[0]) * m.inv_cell, (p0.y - m.lo[1]) * m.inv_cell,
+                        (p0.z - m.lo[2]) * m.inv_cell};
+    bool inside = true;
+    int ci[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      inside = inside && (t[a] >= 0.f) && (t[a] < (float)m.dims[a]);
+      ci[a] = inside ? (int)t[a] : 0;
+      if (ci[a] >= m.dims[a]) ci[a] = m.dims[a] - 1;
+    }
+    if (!inside) return false;
+    const uint32_t cell = ((uint32_t)ci[2] * (uint32_t)m.dims[1] + (uint32_t)ci[1]) * (uint32_t)m.dims[0] + (uint32_t)ci[0];
+    first = __ldg(&m.cell_start[cell]);
+    last = __ldg(&m.cell_start[cell + 1]);
+    list = m.cell_faces;
+  }
+  for (uint32_t k = first; k < last; ++k) {
+    const uint32_t f = list ? __ldg(&list[k]) : k;
+    test_face(m, f, p0, p1, d, dlen, h);
+  }
+  return h.any;
+}
+
+// Leapfrog + collision loop of sph.cl:64-112 (advection.cl:6-23,
+// collisions.cl:91-129), capped at max_iters passes; writes the new state
+// into `out` (same slots) and accumulates the next bounding box.
+__global__ void __launch_bounds__(kBlock)
+    k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out, DevMesh m, Consts c,
+             uint32_t max_iters, uint32_t* __restrict__ bbox, uint32_t* __restrict__ status,
+             unsigned long long* __restrict__ capped_count) {
+  const float qnan = __int_as_float(0x7FC00000);
+  float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float remaining = XMUL(c.time_delta, c.scale);
+    V3 pos = v3(in.pos[i]);
+    const V3 vh_old = v3(in.ivel[i]);
+    V3 v = vh_old;
+    V3 a = v3(acc[i]);
+    bool capped = false;
+    for (uint32_t it = 0;; ++it) {
+      V3 nv = {XADD(v.x, XMUL(a.x, remaining)), XADD(v.y, XMUL(a.y, remaining)),
+               XADD(v.z, XMUL(a.z, remaining))};
+      const float sp = xnorm(nv);
+      if (sp > c.vmax)
+        nv = {XMUL(XDIV(nv.x, sp), c.vmax), XMUL(XDIV(nv.y, sp), c.vmax), XMUL(XDIV(nv.z, sp), c.vmax)};
+      const V3 np = {XADD(pos.x, XMUL(nv.x, remaining)), XADD(pos.y, XMUL(nv.y, remaining)),
+                     XADD(pos.z, XMUL(nv.z, remaining))};
+      Hit h;
+      const bool hit = nearest_hit(m, pos, np, h);
+      float elapsed = remaining;
+      V3 opos = np, ov = nv;
+      if (hit) {
+        opos = {XSUB(h.point.x, XMUL(h.normal.x, 0.001f)), XSUB(h.point.y, XMUL(h.normal.y, 0.001f)),
+                XSUB(h.point.z, XMUL(h.normal.z, 0.001f))};
+        const float k = XMUL(XADD(1.f, XDIV(XMUL(c.restitution, h.depth), XMUL(remaining, xnorm(nv)))),
+                             xdot(nv, h.normal));
+        ov = {XSUB(nv.x, XMUL(k, h.normal.x)), XSUB(nv.y, XMUL(k, h.normal.y)),
+              XSUB(nv.z, XMUL(k, h.normal.z))};
+        elapsed = XMUL(remaining, XDIV(xnorm(xsub3(opos, pos)), xnorm(xsub3(np, pos))));
+      }
+      pos = opos;
+      v = ov;
+      remaining = XSUB(remaining, elapsed);
+      a = {0.f, 0.f, 0.f};
+      if (!hit) break;
+      if (it + 1 >= max_iters) {
+        capped = true;
+        break;
+      }
+    }
+    if (capped) {
+      atomicOr(status, kFlagCollisionCap);
+      atomicAdd(capped_count, 1ull);
+    }
+    out.pos[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
+    out.ivel[i] = make_float4(v.x, v.y, v.z, 0.f);
+    out.vel[i] = make_float4(XDIV(XADD(vh_old.x, v.x), 2.f), XDIV(XADD(vh_old.y, v.y), 2.f),
+                             XDIV(XADD(vh_old.z, v.z), 2.f), 0.f);
+    if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
+    lo = make_float3(fminf(lo.x, pos.x), fminf(lo.y, pos.y), fminf(lo.z, pos.z));
+    hi = make_float3(fmaxf(hi.x, pos.x), fmaxf(hi.y, pos.y), fmaxf(hi.z, pos.z));
+  }
+  bbox_accumulate(lo, hi, bbox);
+}
+
+// Dense reference cell table from the sorted keys: table[c] = lower_bound(c).
+__global__ void k_dense_table(const uint32_t* __restrict__ keys_base, uint32_t n,
+                              const DevGrid* __restrict__ grid, uint32_t* __restrict__ table) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t cells = grid->cells;
+  if (c >= cells) return;
+  const uint32_t* keys = keys_base + (size_t)(sorted_sel(*grid)) * n;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t mid = lo + (hi - lo) / 2;
+    if (keys[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  table[c] = lo;
+}
+
+}  // namespace clsph

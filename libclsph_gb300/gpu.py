@@ -1,0 +1,224 @@
+"""ctypes binding of the C ABI in include/clsph_gpu.h.
+
+`GpuSolver` owns one device handle: create -> set_mesh -> upload -> step ->
+download. It is the thin layer the Python mirror of `sph_simulation`
+(simulation.py), the tests and bench.py use; there is no CPU fallback: if the
+CUDA library or a device is missing, construction raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .layout import PARAMS, PARTICLE, TERMS
+
+_LIB = None
+
+STAGE_GRID, STAGE_SORT, STAGE_DENSITY, STAGE_FORCES, STAGE_ADVECT = 1, 2, 3, 4, 5
+WARN_GRID_OVERFLOW, WARN_COLLISION_CAP, WARN_NONFINITE = 1, 2, 4
+
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+
+# (name, restype, argtypes) of every symbol include/clsph_gpu.h declares
+SIGNATURES = [
+    ("clsph_gpu_create", ctypes.c_int, [_vp, _vp, _u32, ctypes.POINTER(_vp)]),
+    ("clsph_gpu_destroy", ctypes.c_int, [_vp]),
+    ("clsph_gpu_set_stream", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_set_mesh", ctypes.c_int, [_vp, _vp, _vp, _u32, _vp, _u32]),
+    ("clsph_gpu_upload", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_download", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_step", ctypes.c_int, [_vp, _u32]),
+    ("clsph_gpu_step_until", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("clsph_gpu_sync", ctypes.c_int, [_vp, ctypes.POINTER(_u32)]),
+    ("clsph_gpu_get_parameters", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_read_keys", ctypes.c_int, [_vp, _vp, _vp]),
+    ("clsph_gpu_read_cell_table", ctypes.c_int, [_vp, _vp, ctypes.c_uint64]),
+    ("clsph_gpu_read_fields", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("clsph_gpu_read_ids", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("clsph_gpu_kernel_times", ctypes.c_int,
+     [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _vp, _vp, ctypes.POINTER(ctypes.c_int)]),
+    ("clsph_gpu_counters", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_last_error", ctypes.c_char_p, []),
+]
+
+
+def lib_path() -> Path:
+    return Path(__file__).resolve().parent / "_lib" / "libclsph_gpu.so"
+
+
+def load_library(build: bool = False) -> ctypes.CDLL:
+    """Loads libclsph_gpu.so (building it first if asked). Raises if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build or not path.exists():
+        if not build:
+            raise RuntimeError(
+                f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(the CUDA engine has no CPU fallback)")
+        from .build import build_gpu
+        build_gpu()
+    lib = ctypes.CDLL(str(path))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+class ClsphError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+def _check(fn: str, code: int) -> None:
+    if code != 0:
+        msg = (_LIB.clsph_gpu_last_error() or b"").decode(errors="replace")
+        raise ClsphError(fn, code, msg)
+
+
+def _a(x: np.ndarray) -> int:
+    if not x.flags["C_CONTIGUOUS"]:
+        raise ValueError("buffers passed to the C ABI must be C-contiguous")
+    return x.ctypes.data
+
+
+class GpuSolver:
+    """One SPH scene on the current CUDA device (include/clsph_gpu.h)."""
+
+    def __init__(self, params, terms, n: int | None = None, mesh=None):
+        self.lib = load_library()
+        self.params = np.array(params, dtype=PARAMS).reshape(1).copy()
+        self.terms = np.array(terms, dtype=TERMS).reshape(1).copy()
+        self.n = int(n if n is not None else self.params["particles_count"][0])
+        self.params["particles_count"] = self.n
+        handle = _vp()
+        _check("clsph_gpu_create",
+               self.lib.clsph_gpu_create(_a(self.params), _a(self.terms), self.n,
+                                         ctypes.byref(handle)))
+        self.h = handle
+        if mesh is not None:
+            self.set_mesh(mesh)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.clsph_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------ set-up
+    def set_stream(self, stream_handle: int | None) -> None:
+        _check("clsph_gpu_set_stream", self.lib.clsph_gpu_set_stream(self.h, stream_handle))
+
+    def set_mesh(self, mesh) -> None:
+        normals = np.ascontiguousarray(mesh["face_normals"], dtype=np.float32)
+        verts = np.ascontiguousarray(mesh["vertices"], dtype=np.float32)
+        idx = np.ascontiguousarray(mesh["indices"], dtype=np.uint32)
+        faces = len(idx) // 3
+        if faces == 0:
+            _check("clsph_gpu_set_mesh", self.lib.clsph_gpu_set_mesh(self.h, None, None, 0, None, 0))
+            return
+        _check("clsph_gpu_set_mesh",
+               self.lib.clsph_gpu_set_mesh(self.h, _a(normals), _a(verts), len(verts) // 3, _a(idx),
+                                           faces))
+
+    # ------------------------------------------------------------ transfers
+    def upload(self, particles: np.ndarray) -> None:
+        p = np.ascontiguousarray(particles, dtype=PARTICLE)
+        if len(p) != self.n:
+            raise ValueError(f"expected {self.n} particles, got {len(p)}")
+        _check("clsph_gpu_upload", self.lib.clsph_gpu_upload(self.h, _a(p)))
+        # the copy is asynchronous; keep the source alive until the next sync
+        self._pinned_src = p
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.zeros(self.n, dtype=PARTICLE) if out is None else out
+        _check("clsph_gpu_download", self.lib.clsph_gpu_download(self.h, _a(out)))
+        return out
+
+    # ------------------------------------------------------------ stepping
+    def step(self, substeps: int = 1) -> None:
+        _check("clsph_gpu_step", self.lib.clsph_gpu_step(self.h, substeps))
+
+    def step_until(self, stage: int) -> None:
+        _check("clsph_gpu_step_until", self.lib.clsph_gpu_step_until(self.h, stage))
+
+    def sync(self) -> int:
+        flags = _u32(0)
+        _check("clsph_gpu_sync", self.lib.clsph_gpu_sync(self.h, ctypes.byref(flags)))
+        return flags.value
+
+    # ------------------------------------------------------------ inspection
+    def parameters(self) -> np.void:
+        out = np.zeros(1, dtype=PARAMS)
+        _check("clsph_gpu_get_parameters", self.lib.clsph_gpu_get_parameters(self.h, _a(out)))
+        return out[0]
+
+    def keys(self):
+        keys = np.zeros(self.n, dtype=np.uint32)
+        perm = np.zeros(self.n, dtype=np.uint32)
+        _check("clsph_gpu_read_keys", self.lib.clsph_gpu_read_keys(self.h, _a(keys), _a(perm)))
+        return keys, perm
+
+    def cell_table(self) -> np.ndarray:
+        cells = int(self.parameters()["grid_cell_count"])
+        table = np.zeros(max(cells, 1), dtype=np.uint32)
+        _check("clsph_gpu_read_cell_table",
+               self.lib.clsph_gpu_read_cell_table(self.h, _a(table), cells))
+        return table[:cells]
+
+    def fields(self):
+        rho = np.zeros(self.n, dtype=np.float32)
+        prs = np.zeros(self.n, dtype=np.float32)
+        acc = np.zeros((self.n, 4), dtype=np.float32)
+        _check("clsph_gpu_read_fields",
+               self.lib.clsph_gpu_read_fields(self.h, _a(rho), _a(prs), _a(acc)))
+        return rho, prs, acc[:, :3]
+
+    def ids(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.uint32)
+        _check("clsph_gpu_read_ids", self.lib.clsph_gpu_read_ids(self.h, _a(out)))
+        return out
+
+    def set_profiling(self, on: bool) -> None:
+        _check("clsph_gpu_set_profiling", self.lib.clsph_gpu_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_times(self) -> dict:
+        k = 32
+        stride = 32
+        names = ctypes.create_string_buffer(k * stride)
+        ms = np.zeros(k, dtype=np.float32)
+        counts = np.zeros(k, dtype=np.uint32)
+        nk = ctypes.c_int(0)
+        _check("clsph_gpu_kernel_times",
+               self.lib.clsph_gpu_kernel_times(self.h, k, names, stride, _a(ms), _a(counts),
+                                               ctypes.byref(nk)))
+        out = {}
+        for i in range(min(nk.value, k)):
+            name = names.raw[i * stride:(i + 1) * stride].split(b"\0", 1)[0].decode()
+            out[name] = (float(ms[i]), int(counts[i]))
+        return out
+
+    def counters(self) -> dict:
+        c = np.zeros(3, dtype=np.uint64)
+        _check("clsph_gpu_counters", self.lib.clsph_gpu_counters(self.h, _a(c)))
+        return {"substeps": int(c[0]), "collision_capped": int(c[1]), "launches": int(c[2])}

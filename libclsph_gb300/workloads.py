@@ -1,0 +1,186 @@
+"""Seeded synthetic scenes of the benchmark shapes.
+
+No public dataset is involved: every workload is generated here from a seed.
+
+* `dam_break(32)`: 32,768 particles as a 32^3 lattice (spacing h/2, jitter
+  +-1 % of the spacing) in a closed 1 x 1 x 1 m box (12 triangles); water
+  constants of fluid_properties/water.json, gravity -9.81, m = 0.05 kg.
+* `dam_break(128, box=(4, 2, 2))`: 1,048,576 particles (128^3 lattice) in the
+  left quarter (x in [0, 1] m) of a 4 x 2 x 2 m box; the particle mass is
+  chosen so that h = 1/64 m and the block fits at spacing h/2.
+* `pour(...)`: a 64 x 64 x L column falling at 2 m/s (+-5 % per-particle
+  noise) onto a 256 x 256-quad heightfield (131,072 triangles, seeded sum of
+  four sinusoids, amplitude 0.2 m) inside a 4 x 4 x 2 m box.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .layout import PARAMS, PARTICLE, particles_from_arrays
+from .settings import WATER, DEFAULT_SIM, settings_from_dicts
+
+
+@dataclass
+class Scene:
+    name: str
+    params: np.void
+    terms: np.void
+    particles: np.ndarray
+    mesh: dict
+    steps: int
+    info: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return len(self.particles)
+
+
+def face_normals(vertices: np.ndarray, indices: np.ndarray) -> np.ndarray:
+    """Unit normals from the cross product (libclsph/scene.cpp:51-80), float32."""
+    v = np.asarray(vertices, dtype=np.float32).reshape(-1, 3)
+    t = v[np.asarray(indices, dtype=np.int64).reshape(-1, 3)]
+    u = (t[:, 1] - t[:, 0]).astype(np.float32)
+    w = (t[:, 2] - t[:, 0]).astype(np.float32)
+    n = np.stack([u[:, 1] * w[:, 2] - u[:, 2] * w[:, 1],
+                  u[:, 2] * w[:, 0] - u[:, 0] * w[:, 2],
+                  u[:, 0] * w[:, 1] - u[:, 1] * w[:, 0]], axis=1).astype(np.float32)
+    length = np.sqrt((n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]).astype(np.float32)
+    return (n / length[:, None]).astype(np.float32).ravel()
+
+
+def make_mesh(vertices, indices) -> dict:
+    v = np.ascontiguousarray(np.asarray(vertices, dtype=np.float32).ravel())
+    i = np.ascontiguousarray(np.asarray(indices, dtype=np.uint32).ravel())
+    return {"vertices": v, "indices": i, "face_normals": face_normals(v, i)}
+
+
+def box_mesh(lo, hi) -> dict:
+    """Closed axis-aligned box, 12 triangles."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0),
+         (x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (3, 7, 6, 2), (0, 4, 7, 3), (1, 2, 6, 5)]
+    tris = []
+    for a, b, c, d in quads:
+        tris += [a, b, c, a, c, d]
+    return make_mesh(v, tris)
+
+
+def merge_meshes(*meshes) -> dict:
+    verts, idx, off = [], [], 0
+    for m in meshes:
+        v = m["vertices"].reshape(-1, 3)
+        verts.append(v)
+        idx.append(m["indices"].astype(np.int64) + off)
+        off += len(v)
+    return make_mesh(np.concatenate(verts), np.concatenate(idx))
+
+
+def heightfield_mesh(lo_xz, hi_xz, quads, base_y, amplitude, seed) -> dict:
+    """quads x quads grid, two triangles per quad, height = sum of 4 seeded sinusoids."""
+    rng = np.random.default_rng(seed)
+    kx = rng.uniform(0.5, 3.0, 4) * 2 * math.pi / (hi_xz[0] - lo_xz[0])
+    kz = rng.uniform(0.5, 3.0, 4) * 2 * math.pi / (hi_xz[1] - lo_xz[1])
+    ph = rng.uniform(0, 2 * math.pi, 4)
+    amp = rng.uniform(0.5, 1.0, 4)
+    amp *= amplitude / amp.sum()
+    xs = np.linspace(lo_xz[0], hi_xz[0], quads + 1)
+    zs = np.linspace(lo_xz[1], hi_xz[1], quads + 1)
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    Y = base_y + sum(amp[k] * np.sin(kx[k] * X + kz[k] * Z + ph[k]) for k in range(4))
+    verts = np.stack([X, Y, Z], -1).reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(quads), np.arange(quads), indexing="ij")
+    a = (i * (quads + 1) + j).ravel()
+    b = a + 1
+    c = a + quads + 1
+    d = c + 1
+    tris = np.stack([a, c, b, b, c, d], -1).reshape(-1)
+    return make_mesh(verts, tris)
+
+
+def water_settings(n: int, mass: float = 0.05, gravity: float = -9.81, **fluid_overrides):
+    fluid = dict(WATER, **fluid_overrides)
+    sim = dict(DEFAULT_SIM, particles_count=n, particle_mass=mass,
+               constant_acceleration={"x": 0.0, "y": gravity, "z": 0.0})
+    return settings_from_dicts(fluid, sim)
+
+
+def mass_for_h(h: float, rho0: float = WATER["fluid_density"], k: int = 20) -> float:
+    """Particle mass that makes load_settings derive smoothing radius h."""
+    return h ** 3 * 4.0 * math.pi * rho0 / (3.0 * k)
+
+
+def lattice(shape, spacing, origin, jitter_frac, rng) -> np.ndarray:
+    nx, ny, nz = shape
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1)
+    g = g.reshape(-1, 3).astype(np.float64)
+    pos = np.asarray(origin, dtype=np.float64) + (g + 0.5) * spacing
+    pos += rng.uniform(-jitter_frac * spacing, jitter_frac * spacing, pos.shape)
+    return pos.astype(np.float32)
+
+
+def dam_break(side: int = 32, box=(1.0, 1.0, 1.0), seed: int = 1, mass: float | None = None,
+              steps: int = 1000, jitter: float = 0.01) -> Scene:
+    n = side ** 3
+    if mass is None:
+        mass = 0.05 if box == (1.0, 1.0, 1.0) else mass_for_h(1.0 / 64.0)
+    st = water_settings(n, mass=mass)
+    h = float(st.params["h"])
+    s = h / 2
+    rng = np.random.default_rng(seed)
+    block = side * s
+    if box == (1.0, 1.0, 1.0):
+        origin = ((1.0 - block) / 2, (1.0 - block) / 2, (1.0 - block) / 2)
+    else:  # left quarter, on the floor, centred in z
+        origin = (0.0, 0.0, (box[2] - block) / 2)
+    pos = lattice((side, side, side), s, origin, jitter, rng)
+    parts = particles_from_arrays(pos)
+    return Scene(f"dam_break_{n}", st.params, st.terms, parts, box_mesh((0, 0, 0), box), steps,
+                 {"h": h, "spacing": s, "mass": mass, "box": list(box), "seed": seed})
+
+
+def pour(cross: int = 64, length: int = 1024, quads: int = 256, seed: int = 3,
+         steps: int = 3000) -> Scene:
+    box = (4.0, 2.0, 4.0)  # x, y (up), z
+    top = 1.9
+    bottom_y = 0.5
+    s = (top - bottom_y) / length
+    h = 2 * s
+    mass = mass_for_h(h)
+    n = cross * cross * length
+    st = water_settings(n, mass=mass)
+    rng = np.random.default_rng(seed)
+    origin = (box[0] / 2 - cross * s / 2, bottom_y, box[2] / 2 - cross * s / 2)
+    pos = lattice((cross, length, cross), s, origin, 0.01, rng)
+    vel = np.zeros_like(pos)
+    vel[:, 1] = -2.0 * (1.0 + rng.uniform(-0.05, 0.05, n))
+    parts = particles_from_arrays(pos, vel, vel)
+    field_mesh = heightfield_mesh((0.0, 0.0), (box[0], box[2]), quads, 0.25, 0.2, seed)
+    mesh = merge_meshes(field_mesh, box_mesh((0, 0, 0), box))
+    return Scene(f"pour_{n}", st.params, st.terms, parts, mesh, steps,
+                 {"h": float(st.params["h"]), "spacing": s, "mass": mass, "faces": len(mesh["indices"]) // 3,
+                  "seed": seed})
+
+
+def small_block(n_side: int = 8, seed: int = 0, box=(1.0, 1.0, 1.0), offset=(0.3, 0.05, 0.3),
+                velocity_sigma: float = 0.0, spacing_frac: float = 0.5) -> Scene:
+    """A small jittered block for parity tests (sizes the oracle finishes fast)."""
+    n = n_side ** 3
+    st = water_settings(n)
+    h = float(st.params["h"])
+    rng = np.random.default_rng(seed)
+    pos = lattice((n_side,) * 3, h * spacing_frac, offset, 0.01, rng)
+    vel = rng.normal(0.0, velocity_sigma, pos.shape).astype(np.float32) if velocity_sigma else None
+    parts = particles_from_arrays(pos, vel, vel)
+    return Scene(f"block_{n}", st.params, st.terms, parts, box_mesh((0, 0, 0), box), 10,
+                 {"h": h, "seed": seed})
+
+
+__all__ = ["Scene", "box_mesh", "heightfield_mesh", "merge_meshes", "make_mesh", "face_normals",
+           "water_settings", "mass_for_h", "dam_break", "pour", "small_block", "lattice",
+           "PARAMS", "PARTICLE"]

@@ -1,0 +1,143 @@
+"""Generates the golden fixtures of tests/golden/ from oracle/_ref.
+
+oracle/_ref is the reference's own kernel sources (libclsph/kernels/*.cl,
+libclsph/common/*.h) compiled as C++ through oracle/ref_shim, driven by a
+restatement of libclsph/sph_simulation.cpp's substep. Each fixture holds the
+inputs of one substep (parameter block, kernel constants, particle AoS,
+mesh) and every output the reference produces for it: the grid parameters,
+the stable-sort permutation, the dense cell table, the AoS after the sort,
+after density_pressure, after forces, and after advection_collision.
+
+Run in the development container (needs the reference sources):
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from libclsph_gb300 import workloads as W  # noqa: E402
+from libclsph_gb300.layout import particles_from_arrays  # noqa: E402
+from libclsph_gb300.settings import WATER, DEFAULT_SIM, settings_from_dicts  # noqa: E402
+from oracle import RefBuild, build_ref  # noqa: E402
+
+REF_ROOT = Path("/root/reference")
+MUCUS = {"fluid_density": 1000, "dynamic_viscosity": 36, "restitution": 0.5, "k": 5,
+         "surface_tension_threshold": 5, "surface_tension": 6,
+         "particles_inside_influence_radius": 40}
+
+
+def obj_mesh(name: str) -> dict:
+    """A scene of the reference's scenes/ folder through the project's OBJ
+    reader (same vertex/face order as tinyobj 0.9.6)."""
+    from libclsph_gb300.scene import Scene
+
+    sc = Scene()
+    if not sc.load(name, base=REF_ROOT / "scenes"):
+        raise RuntimeError(f"cannot load {name}")
+    return {"vertices": np.asarray(sc.vertices, np.float32),
+            "indices": np.asarray(sc.indices, np.uint32),
+            "face_normals": np.asarray(sc.face_normals, np.float32)}
+
+
+def settings(n, fluid=WATER, **sim_overrides):
+    sim = dict(DEFAULT_SIM, particles_count=n, **sim_overrides)
+    return settings_from_dicts(fluid, sim)
+
+
+def case_default_lattice():
+    """The reference's own initial condition (init_particles cube lattice),
+    512 particles, water + default properties, scenes/cube.obj."""
+    from oracle import Oracle
+
+    st = settings(512)
+    parts = Oracle().init_lattice(512, st.initial_volume)
+    return "default_lattice_cube_512", st, parts, obj_mesh("cube.obj"), 1
+
+
+def case_box_floor():
+    """4096 particles with random velocities on the floor of scenes/box.obj."""
+    st = settings(4096, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
+    h = float(st.params["h"])
+    rng = np.random.default_rng(11)
+    pos = W.lattice((16, 16, 16), h / 2, (-0.25, -1.9995, -0.25), 0.01, rng)
+    vel = rng.normal(0, 1.5, pos.shape).astype(np.float32)
+    vel[:, 1] -= 2.0
+    return "box_floor_4096", st, particles_from_arrays(pos, vel, vel), obj_mesh("box.obj"), 1
+
+
+def case_mucus_corner():
+    """1000 mucus particles (restitution 0.5) driven into a corner of a unit box."""
+    st = settings(1000, fluid=MUCUS, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
+    h = float(st.params["h"])
+    rng = np.random.default_rng(12)
+    pos = W.lattice((10, 10, 10), h / 2, (0.0004, 0.0004, 0.0004), 0.01, rng)
+    vel = (-np.abs(rng.normal(0, 3.0, pos.shape))).astype(np.float32)
+    return ("mucus_corner_1000", st, particles_from_arrays(pos, vel, vel),
+            W.box_mesh((0, 0, 0), (1, 1, 1)), 1)
+
+
+def case_coincident():
+    """Coincident pairs (the r ~ 0 branch of spiky_gradient) and particles on
+    exact cell boundaries."""
+    st = settings(729)
+    h = float(st.params["h"])
+    rng = np.random.default_rng(13)
+    pos = W.lattice((9, 9, 9), h / 2, (0.3, 0.3, 0.3), 0.0, rng).astype(np.float32)
+    pos[1::7] = pos[0::7][: len(pos[1::7])]  # duplicate positions
+    vel = rng.normal(0, 0.2, pos.shape).astype(np.float32)
+    return ("coincident_729", st, particles_from_arrays(pos, vel, vel),
+            W.box_mesh((0, 0, 0), (1, 1, 1)), 1)
+
+
+def case_trajectory():
+    """Five substeps of a 27^3 block dropping in a unit box (final AoS)."""
+    st = settings(19683, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
+    h = float(st.params["h"])
+    rng = np.random.default_rng(14)
+    pos = W.lattice((27, 27, 27), h / 2, (0.05, 0.02, 0.05), 0.01, rng)
+    vel = rng.normal(0, 0.3, pos.shape).astype(np.float32)
+    return ("trajectory_19683_x5", st, particles_from_arrays(pos, vel, vel),
+            W.box_mesh((0, 0, 0), (1, 1, 1)), 5)
+
+
+CASES = [case_default_lattice, case_box_floor, case_mucus_corner, case_coincident, case_trajectory]
+
+
+def main() -> None:
+    if build_ref() is None:
+        raise SystemExit("reference sources not found; fixtures are generated in the dev container")
+    ref = RefBuild()
+    manifest = {}
+    for make in CASES:
+        name, st, parts, mesh, steps = make()
+        out = {"params": np.array(st.params).reshape(1), "terms": np.array(st.terms).reshape(1),
+               "particles": parts, "vertices": mesh["vertices"], "indices": mesh["indices"],
+               "face_normals": mesh["face_normals"], "steps": np.array([steps])}
+        if steps == 1:
+            r = ref.step(st.params, st.terms, parts, mesh)
+            out.update(params_out=np.array(r.params).reshape(1), perm=r.perm, table=r.table,
+                       sorted=r.sorted, density=r.density, forces=r.forces, final=r.final,
+                       capped=np.array([r.capped]))
+        else:
+            cur = parts
+            for _ in range(steps):
+                cur = ref.step(st.params, st.terms, cur, mesh).final
+            out.update(final=cur)
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+        manifest[name] = {"n": int(len(parts)), "steps": steps,
+                          "faces": int(len(mesh["indices"]) // 3)}
+        print(name, manifest[name])
+    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+
+
+if __name__ == "__main__":
+    main()
