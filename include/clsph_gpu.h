@@ -90,6 +90,12 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
                      clsph_gpu** out);
 int clsph_gpu_destroy(clsph_gpu* h);
 
+/* Cap of the advect/collide loop per particle and substep (default 1024).
+ * The reference loop is unbounded (kernels/sph.cl:82-101); a particle that
+ * reaches the cap keeps its last position and CLSPH_WARN_COLLISION_CAP is
+ * raised. */
+int clsph_gpu_set_collision_cap(clsph_gpu* h, uint32_t max_iterations);
+
 /* Launch stream (a cudaStream_t); NULL selects the handle's own stream. */
 int clsph_gpu_set_stream(clsph_gpu* h, void* cuda_stream);
 

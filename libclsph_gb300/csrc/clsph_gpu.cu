@@ -464,6 +464,12 @@ int clsph_gpu_destroy(clsph_gpu* h) {
   return CLSPH_OK;
 }
 
+int clsph_gpu_set_collision_cap(clsph_gpu* h, uint32_t max_iterations) {
+  if (!h || max_iterations == 0) return fail(CLSPH_ERR_ARGUMENT, "set_collision_cap: bad argument");
+  h->max_iters = max_iterations;
+  return CLSPH_OK;
+}
+
 int clsph_gpu_set_stream(clsph_gpu* h, void* stream) {
   if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_stream: null handle");
   CUDA_TRY(cudaStreamSynchronize(h->stream));

@@ -27,6 +27,7 @@ _u32 = ctypes.c_uint32
 SIGNATURES = [
     ("clsph_gpu_create", ctypes.c_int, [_vp, _vp, _u32, ctypes.POINTER(_vp)]),
     ("clsph_gpu_destroy", ctypes.c_int, [_vp]),
+    ("clsph_gpu_set_collision_cap", ctypes.c_int, [_vp, _u32]),
     ("clsph_gpu_set_stream", ctypes.c_int, [_vp, _vp]),
     ("clsph_gpu_set_mesh", ctypes.c_int, [_vp, _vp, _vp, _u32, _vp, _u32]),
     ("clsph_gpu_upload", ctypes.c_int, [_vp, _vp]),
@@ -128,6 +129,9 @@ class GpuSolver:
     # ------------------------------------------------------------ set-up
     def set_stream(self, stream_handle: int | None) -> None:
         _check("clsph_gpu_set_stream", self.lib.clsph_gpu_set_stream(self.h, stream_handle))
+
+    def set_collision_cap(self, iterations: int) -> None:
+        _check("clsph_gpu_set_collision_cap", self.lib.clsph_gpu_set_collision_cap(self.h, iterations))
 
     def set_mesh(self, mesh) -> None:
         normals = np.ascontiguousarray(mesh["face_normals"], dtype=np.float32)

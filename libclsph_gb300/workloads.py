@@ -5,9 +5,11 @@ No public dataset is involved: every workload is generated here from a seed.
 * `dam_break(32)`: 32,768 particles as a 32^3 lattice (spacing h/2, jitter
   +-1 % of the spacing) in a closed 1 x 1 x 1 m box (12 triangles); water
   constants of fluid_properties/water.json, gravity -9.81, m = 0.05 kg.
-* `dam_break(128, box=(4, 2, 2))`: 1,048,576 particles (128^3 lattice) in the
-  left quarter (x in [0, 1] m) of a 4 x 2 x 2 m box; the particle mass is
-  chosen so that h = 1/64 m and the block fits at spacing h/2.
+* `dam_break((128, 128, 64), box=(4, 2, 2))`: 1,048,576 particles as a
+  128 x 128 x 64 lattice (1 m wide in x, 1 m tall, 0.5 m deep; a 128^3
+  lattice would hold 2,097,152) in the left quarter (x in [0, 1] m) of a
+  4 x 2 x 2 m box; the particle mass is chosen so that h = 1/64 m and the
+  block fits at spacing h/2.
 * `pour(...)`: a 64 x 64 x L column falling at 2 m/s (+-5 % per-particle
   noise) onto a 256 x 256-quad heightfield (131,072 triangles, seeded sum of
   four sinusoids, amplitude 0.2 m) inside a 4 x 4 x 2 m box.
@@ -124,24 +126,37 @@ def lattice(shape, spacing, origin, jitter_frac, rng) -> np.ndarray:
     return pos.astype(np.float32)
 
 
-def dam_break(side: int = 32, box=(1.0, 1.0, 1.0), seed: int = 1, mass: float | None = None,
+def dam_break(shape=(32, 32, 32), box=(1.0, 1.0, 1.0), seed: int = 1, mass: float | None = None,
               steps: int = 1000, jitter: float = 0.01) -> Scene:
-    n = side ** 3
+    if isinstance(shape, int):
+        shape = (shape, shape, shape)
+    n = int(np.prod(shape))
     if mass is None:
         mass = 0.05 if box == (1.0, 1.0, 1.0) else mass_for_h(1.0 / 64.0)
     st = water_settings(n, mass=mass)
     h = float(st.params["h"])
     s = h / 2
     rng = np.random.default_rng(seed)
-    block = side * s
+    ext = [k * s for k in shape]
     if box == (1.0, 1.0, 1.0):
-        origin = ((1.0 - block) / 2, (1.0 - block) / 2, (1.0 - block) / 2)
+        origin = tuple((1.0 - e) / 2 for e in ext)
     else:  # left quarter, on the floor, centred in z
-        origin = (0.0, 0.0, (box[2] - block) / 2)
-    pos = lattice((side, side, side), s, origin, jitter, rng)
+        origin = (0.0, 0.0, (box[2] - ext[2]) / 2)
+    pos = lattice(tuple(shape), s, origin, jitter, rng)
     parts = particles_from_arrays(pos)
     return Scene(f"dam_break_{n}", st.params, st.terms, parts, box_mesh((0, 0, 0), box), steps,
-                 {"h": h, "spacing": s, "mass": mass, "box": list(box), "seed": seed})
+                 {"h": h, "spacing": s, "mass": mass, "box": list(box), "seed": seed,
+                  "lattice": list(shape)})
+
+
+def dam_break_32k(seed: int = 1) -> Scene:
+    """32,768 particles, 32^3 lattice, 1 m box, 1000 substeps."""
+    return dam_break((32, 32, 32), seed=seed, steps=1000)
+
+
+def dam_break_1m(seed: int = 1) -> Scene:
+    """1,048,576 particles, 128 x 128 x 64 lattice, 4 x 2 x 2 m box, 2000 substeps."""
+    return dam_break((128, 128, 64), box=(4.0, 2.0, 2.0), seed=seed, steps=2000)
 
 
 def pour(cross: int = 64, length: int = 1024, quads: int = 256, seed: int = 3,
@@ -182,5 +197,5 @@ def small_block(n_side: int = 8, seed: int = 0, box=(1.0, 1.0, 1.0), offset=(0.3
 
 
 __all__ = ["Scene", "box_mesh", "heightfield_mesh", "merge_meshes", "make_mesh", "face_normals",
-           "water_settings", "mass_for_h", "dam_break", "pour", "small_block", "lattice",
+           "water_settings", "mass_for_h", "dam_break", "dam_break_32k", "dam_break_1m", "pour", "small_block", "lattice",
            "PARAMS", "PARTICLE"]
