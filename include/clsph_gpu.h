@@ -161,6 +161,24 @@ int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_
  * the cap, [2] kernel launches. */
 int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3);
 
+/* Stable sort of n device-resident 32-bit keys that allocates no memory.
+ * No counterpart in the reference: it exists for callers that may not call
+ * cudaMalloc themselves (a host application or framework that owns every
+ * device allocation and forbids raw cudaMalloc/cudaFree, or a real-time loop
+ * that must not allocate after start-up). It is the substep's stable sort
+ * (the 4 x 8-bit LSD radix sort) on caller buffers: keys_out receives the
+ * keys in ascending order, perm_out[s] the input index of sorted slot s
+ * (equal keys keep input order). keys_in must not overlap the outputs.
+ * Scratch comes from one 8.3 MB file-scope __device__ array held by every GPU
+ * that loads the library until exit; n above 1,048,576 is rejected with
+ * CLSPH_ERR_TOO_LARGE. All calls share that array (each clears what must
+ * start at zero): calls whose GPU work overlaps race, so serialise them. The
+ * first call on a device looks the array up (cudaGetSymbolAddress) with that
+ * device current; make it before any stream capture. Asynchronous on
+ * `cuda_stream` (a cudaStream_t, NULL = legacy default stream). */
+int clsph_gpu_sort_keys_noalloc(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
+                                uint32_t n, void* cuda_stream);
+
 /* Text of the last error on this thread. */
 const char* clsph_gpu_last_error(void);
 

@@ -45,7 +45,7 @@ def _run(cmd: list[str]) -> None:
 
 
 def gpu_cmd(extra: list[str] | None = None) -> list[str]:
-    srcs = [str(CSRC / "clsph_gpu.cu")]
+    srcs = [str(CSRC / "clsph_gpu.cu"), str(CSRC / "clsph_sort_noalloc.cu")]
     return [
         _nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
         f"-I{INCLUDE}", f"-I{CSRC}", *(extra or []), "-o", str(GPU_SO), *srcs,

@@ -86,6 +86,9 @@ float pown_f(float x, int k) {
 
 }  // namespace
 
+// Error text for clsph_gpu_last_error from the library's other translation units.
+void clsph_set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct clsph_gpu {
   int device = 0;
   cudaStream_t own_stream = nullptr;

@@ -44,6 +44,7 @@ SIGNATURES = [
     ("clsph_gpu_kernel_times", ctypes.c_int,
      [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _vp, _vp, ctypes.POINTER(ctypes.c_int)]),
     ("clsph_gpu_counters", ctypes.c_int, [_vp, _vp]),
+    ("clsph_gpu_sort_keys_noalloc", ctypes.c_int, [_vp, _vp, _vp, _u32, _vp]),
     ("clsph_gpu_last_error", ctypes.c_char_p, []),
 ]
 
