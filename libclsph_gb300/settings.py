@@ -18,6 +18,8 @@ reference's float/double mixing:
 
 from __future__ import annotations
 
+import ctypes
+import ctypes.util
 import json
 import math
 from dataclasses import dataclass
@@ -28,6 +30,15 @@ import numpy as np
 from .layout import PARAMS, TERMS
 
 f32 = np.float32
+
+_libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+_libm.cbrtf.restype = ctypes.c_float
+_libm.cbrtf.argtypes = [ctypes.c_float]
+
+
+def cbrtf(x) -> np.float32:
+    """C's cbrtf (the reference calls it; numpy's float32 cbrt can differ by an ulp)."""
+    return f32(_libm.cbrtf(float(f32(x))))
 
 FLUID_KEYS = ["fluid_density", "dynamic_viscosity", "restitution", "k",
               "surface_tension_threshold", "surface_tension", "particles_inside_influence_radius"]
@@ -62,7 +73,7 @@ def derive(params: np.void, influence_count: int) -> tuple[np.void, np.void, flo
     total_mass = f32(f32(n) * m)
     volume = f32(total_mass / f32(p["fluid_density"][0]))
     q = float(f32(3.0) * f32(f32(influence_count) * f32(volume / f32(n)))) / (4.0 * math.pi)
-    h = f32(np.cbrt(f32(q)))
+    h = cbrtf(q)
     td = f32(f32(1.0) / f32(p["target_fps"][0]))
     p["total_mass"] = total_mass
     p["h"] = h

@@ -1,0 +1,191 @@
+"""Python mirror of libclsph's sph_simulation and houdini_file_saver.
+
+`Simulation` keeps the reference's surface (libclsph/sph_simulation.h:8-52):
+`load_settings(fluid_file, parameters_file)`, `simulate(frame_count=0)`,
+`parameters`, `precomputed_terms`, `pre_frame` / `post_frame` callbacks
+`(particles, parameters, full_frame)`, `write_intermediate_frames`,
+`serialize`, `initial_volume`, `current_scene`. Substeps run on the GPU
+engine (gpu.GpuSolver); the particle AoS is copied to the host only when a
+callback needs it (see `transfers`).
+
+`HoudiniFileSaver` writes the reference's ASCII .geo frames
+(libclsph/file_save_delegates/houdini_file_saver.cpp:25-92).
+"""
+
+from __future__ import annotations
+
+import math
+import os
+from pathlib import Path
+from typing import Callable, Optional
+
+import numpy as np
+
+from .layout import PARAMS, PARTICLE, TERMS
+from .scene import Scene
+from .settings import cbrtf, load_settings
+
+f32 = np.float32
+
+EVERY_SUBSTEP = "every_substep"
+FRAMES_ONLY = "frames_only"
+
+
+def init_lattice(n: int, initial_volume: float) -> np.ndarray:
+    """sph_simulation.cpp:102-148 cube lattice (no last_frame.bin)."""
+    side = int(math.ceil(float(cbrtf(n))))
+    length = cbrtf(initial_volume)
+    gap = f32(length / f32(side))
+    i = np.arange(n, dtype=np.int64)
+    out = np.zeros(n, dtype=PARTICLE)
+    half = f32(length / f32(2.0))
+    out["position"][:, 0] = ((i % side).astype(f32) * gap - half).astype(f32)
+    out["position"][:, 1] = (((i // side) % side).astype(f32) * gap).astype(f32)
+    out["position"][:, 2] = ((i // (side * side)).astype(f32) * gap - half).astype(f32)
+    return out
+
+
+class Simulation:
+    def __init__(self):
+        self.parameters = np.zeros(1, dtype=PARAMS)[0]
+        self.precomputed_terms = np.zeros(1, dtype=TERMS)[0]
+        self.pre_frame: Optional[Callable] = None
+        self.post_frame: Optional[Callable] = None
+        self.write_intermediate_frames = False
+        self.serialize = False
+        self.initial_volume = 0.0
+        self.current_scene = Scene()
+        self.transfers = EVERY_SUBSTEP
+        self.collision_iteration_cap = 1024
+        self.last_particles: Optional[np.ndarray] = None
+
+    def load_settings(self, fluid_file, parameters_file) -> None:
+        st = load_settings(fluid_file, parameters_file)
+        self.parameters = st.params
+        self.precomputed_terms = st.terms
+        self.initial_volume = st.initial_volume
+        self.write_intermediate_frames = st.write_intermediate_frames
+        self.serialize = st.serialize
+
+    def init_particles(self) -> np.ndarray:
+        n = int(self.parameters["particles_count"])
+        if os.path.exists("last_frame.bin"):
+            raw = np.fromfile("last_frame.bin", dtype=np.uint8)
+            if raw.size < n * PARTICLE.itemsize:
+                raise RuntimeError("last_frame.bin is shorter than the particle count")
+            return raw[: n * PARTICLE.itemsize].view(PARTICLE).copy()
+        return init_lattice(n, self.initial_volume)
+
+    def simulate(self, frame_count: int = 0) -> np.ndarray:
+        from .gpu import GpuSolver
+
+        p = self.parameters
+        if frame_count == 0:
+            frame_count = int(math.ceil(float(f32(p["simulation_time"]) * f32(p["target_fps"]))))
+        n = int(p["particles_count"])
+        mesh = self.current_scene.mesh() if self.current_scene.face_count else None
+        particles = self.init_particles()
+        state = {"device_newer": False, "host_dirty": False}
+        with GpuSolver(p, self.precomputed_terms, n, mesh) as gpu:
+            gpu.set_collision_cap(self.collision_iteration_cap)
+            gpu.upload(particles)
+
+            def refresh():
+                if not state["device_newer"]:
+                    return
+                gpu.download(particles)
+                grid = gpu.parameters()
+                for f in ("min_point", "max_point", "grid_size_x", "grid_size_y", "grid_size_z",
+                          "grid_cell_count"):
+                    self.parameters[f] = grid[f]
+                flags = gpu.sync()
+                if flags & 1:
+                    raise RuntimeError("particle grid reached 1024 cells on an axis")
+                state["device_newer"] = False
+
+            def call(cb, full):
+                if cb is None:
+                    return
+                if full or self.transfers == EVERY_SUBSTEP:
+                    refresh()
+                    cb(particles, self.parameters, full)
+                    state["host_dirty"] = True
+                else:
+                    cb(particles, self.parameters, full)
+
+            substeps = 0
+            while f32(substeps) < f32(1.0) / f32(p["simulation_scale"]):
+                substeps += 1
+            for _ in range(frame_count):
+                call(self.pre_frame, True)
+                for _ in range(substeps):
+                    call(self.pre_frame, False)
+                    if state["host_dirty"]:
+                        gpu.upload(particles)
+                        state["host_dirty"] = False
+                    gpu.step(1)
+                    state["device_newer"] = True
+                    call(self.post_frame, False)
+                call(self.post_frame, True)
+            refresh()
+        self.last_particles = particles
+        return particles
+
+
+def _g(x) -> str:
+    """A float printed like std::ostream's default formatting."""
+    return f"{float(f32(x)):g}"
+
+
+def density_color(d):
+    d = f32(d)
+    r = (d - f32(1000)) / f32(1000) if (d > 1000 and d <= 2000) else f32(0)
+    g = f32(1) - d / f32(1000) if (d >= 0 and d < 1000) else f32(0)
+    if 500 <= d <= 1000:
+        b = (d - f32(500)) / f32(500)
+    elif 1000 <= d <= 1500:
+        b = f32(1) - (d - f32(1000)) / f32(500)
+    else:
+        b = f32(0)
+    return f32(r), f32(g), f32(b)
+
+
+class HoudiniFileSaver:
+    """houdini_file_saver (libclsph/file_save_delegates/houdini_file_saver.h:8-20)."""
+
+    def __init__(self, frames_folder_prefix: str):
+        self.frames_folder_prefix = frames_folder_prefix
+        self.frame_count = 0
+
+    def writeFrameToFile(self, particles: np.ndarray, parameters) -> int:
+        self.frame_count += 1
+        name = f"{self.frames_folder_prefix}frames/frame{str(self.frame_count).zfill(9)[-7:]}.geo"
+        n = int(parameters["particles_count"])
+        mass = _g(parameters["particle_mass"])
+        lines = ["PGEOMETRY V5", f"NPoints {n} NPrims 1", "NPointGroups 0 NPrimGroups 1",
+                 "NPointAttrib 3 NVertexAttrib 0 NPrimAttrib 2 NAttrib 0", "PointAttrib",
+                 "v 3 float 1 1 1", "color 3 float 1 1 1", "mass 1 float 1"]
+        pos = particles["position"]
+        vel = particles["velocity"]
+        dens = particles["density"]
+        for i in range(n):
+            r, g, b = density_color(dens[i])
+            lines.append(f"{_g(pos[i, 0])} {_g(pos[i, 1])} {_g(pos[i, 2])} 0 "
+                         f"({_g(vel[i, 0])} {_g(vel[i, 1])} {_g(vel[i, 2])}\t"
+                         f"{_g(r)} {_g(g)} {_g(b)}\t{mass})")
+        lines += ["PrimitiveAttrib", "generator 1 index 1 location1",
+                  "dopobject 1 index 1 /obj/AutoDopNetwork:1",
+                  "Part " + str(n) + "".join(f" {i}" for i in range(n)) + " [0\t0]",
+                  "box_object1 unordered", "1 1", "beginExtra", "endExtra"]
+        try:
+            Path(name).write_text("\n".join(lines) + "\n")
+        except OSError:
+            import sys
+
+            sys.stderr.write(f"Error while writing to {name}\n")
+        return 0
+
+
+def save_last_frame(particles: np.ndarray, path: str = "last_frame.bin") -> None:
+    """The example's serialize step (example/particles.cpp:40-44): raw AoS bytes."""
+    np.ascontiguousarray(particles, dtype=PARTICLE).tofile(path)

@@ -51,7 +51,8 @@ def face_normals(vertices: np.ndarray, indices: np.ndarray) -> np.ndarray:
                   u[:, 2] * w[:, 0] - u[:, 0] * w[:, 2],
                   u[:, 0] * w[:, 1] - u[:, 1] * w[:, 0]], axis=1).astype(np.float32)
     length = np.sqrt((n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]).astype(np.float32)
-    return (n / length[:, None]).astype(np.float32).ravel()
+    with np.errstate(invalid="ignore", divide="ignore"):  # degenerate faces give NaN, as in C
+        return (n / length[:, None]).astype(np.float32).ravel()
 
 
 def make_mesh(vertices, indices) -> dict:

@@ -64,14 +64,14 @@ def case_default_lattice():
 
 
 def case_box_floor():
-    """4096 particles with random velocities on the floor of scenes/box.obj."""
-    st = settings(4096, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
+    """2000 particles with random velocities on the floor of scenes/box.obj."""
+    st = settings(2000, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
     h = float(st.params["h"])
     rng = np.random.default_rng(11)
-    pos = W.lattice((16, 16, 16), h / 2, (-0.25, -1.9995, -0.25), 0.01, rng)
+    pos = W.lattice((20, 5, 20), h / 2, (-0.25, -1.9995, -0.25), 0.01, rng)
     vel = rng.normal(0, 1.5, pos.shape).astype(np.float32)
     vel[:, 1] -= 2.0
-    return "box_floor_4096", st, particles_from_arrays(pos, vel, vel), obj_mesh("box.obj"), 1
+    return "box_floor_2000", st, particles_from_arrays(pos, vel, vel), obj_mesh("box.obj"), 1
 
 
 def case_mucus_corner():
@@ -99,13 +99,13 @@ def case_coincident():
 
 
 def case_trajectory():
-    """Five substeps of a 27^3 block dropping in a unit box (final AoS)."""
-    st = settings(19683, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
+    """Five substeps of a 15^3 block dropping onto the floor of a unit box (final AoS)."""
+    st = settings(3375, constant_acceleration={"x": 0, "y": -9.81, "z": 0})
     h = float(st.params["h"])
     rng = np.random.default_rng(14)
-    pos = W.lattice((27, 27, 27), h / 2, (0.05, 0.02, 0.05), 0.01, rng)
+    pos = W.lattice((15, 15, 15), h / 2, (0.05, 0.0005, 0.05), 0.01, rng)
     vel = rng.normal(0, 0.3, pos.shape).astype(np.float32)
-    return ("trajectory_19683_x5", st, particles_from_arrays(pos, vel, vel),
+    return ("trajectory_3375_x5", st, particles_from_arrays(pos, vel, vel),
             W.box_mesh((0, 0, 0), (1, 1, 1)), 5)
 
 
