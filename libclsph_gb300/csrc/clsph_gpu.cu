@@ -7,6 +7,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -91,6 +92,7 @@ void clsph_set_last_error(const std::string& msg) { g_last_error = msg; }
 
 struct clsph_gpu {
   int device = 0;
+  uint32_t sm_count = 152;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   uint32_t n = 0;
@@ -101,9 +103,13 @@ struct clsph_gpu {
   State st[2]{};
   uint32_t* ids[2]{};
   int ids_sel = 0;
-  float* rho = nullptr;
-  float* prs = nullptr;
+  float4* aux = nullptr;  // (rho, p, m/rho, p/rho^2)
   float4* acc = nullptr;
+  uint32_t* nlist = nullptr;
+  uint32_t* ncount = nullptr;
+  uint32_t* cell_list = nullptr;      // first sorted slot of every occupied cell
+  uint32_t* step_counters = nullptr;  // kStepCounters, zeroed every substep
+  uint32_t nlist_cap = 64;
   uint32_t* keys = nullptr;  // [2n]
   uint32_t* vals = nullptr;  // [2n]
   uint32_t* tile_hist = nullptr;
@@ -151,12 +157,17 @@ struct clsph_gpu {
 
   template <typename Kernel, typename... Args>
   void launch(int cls, Kernel k, dim3 g, dim3 b, Args... args) {
+    launch_smem(cls, k, g, b, 0, args...);
+  }
+
+  template <typename Kernel, typename... Args>
+  void launch_smem(int cls, Kernel k, dim3 g, dim3 b, size_t smem, Args... args) {
     PendingTiming t{cls, nullptr, nullptr};
     if (profiling) {
       t.start = take_event();
       cudaEventRecord(t.start, stream);
     }
-    k<<<g, b, 0, stream>>>(args...);
+    k<<<g, b, smem, stream>>>(args...);
     ++launches;
     if (profiling) {
       t.stop = take_event();
@@ -225,7 +236,7 @@ int enqueue_substep(clsph_gpu* h, int until) {
   const uint32_t n = h->n;
   const uint32_t blocks = grid_blocks(n);
   h->launch(K_GRID_SETUP, k_grid_setup, dim3(1), dim3(256), h->bbox, h->grid, h->params.h,
-            h->status, h->digit_total);
+            h->status, h->digit_total, h->step_counters);
   CUDA_TRY(cudaMemsetAsync(h->ci.keys, 0, sizeof(uint32_t) * h->slots, h->stream));
   h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n, h->grid,
             h->keys);
@@ -242,15 +253,18 @@ int enqueue_substep(clsph_gpu* h, int until) {
   const int src_ids = h->ids_sel, dst_ids = h->ids_sel ^ 1;
   h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
             (const uint32_t*)h->keys, (const uint32_t*)h->vals, h->st[0], h->st[1],
-            (const uint32_t*)h->ids[src_ids], h->ids[dst_ids], h->ci);
+            (const uint32_t*)h->ids[src_ids], h->ids[dst_ids], h->ci, h->cell_list,
+            h->step_counters + kCntCells);
   h->ids_sel = dst_ids;
   if (until <= CLSPH_STAGE_SORT) return 0;
-  h->launch(K_DENSITY, k_density, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
-            (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci, h->consts, h->rho, h->prs);
+  const uint32_t gblocks = (n + kGatherBlock - 1) / kGatherBlock;
+  h->launch(K_DENSITY, k_density, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grid,
+            (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci, h->consts, h->aux,
+            h->nlist, h->ncount, h->nlist_cap);
   if (until <= CLSPH_STAGE_DENSITY) return 0;
-  h->launch(K_FORCES, k_forces, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
-            (const uint32_t*)h->keys, h->st[1], (const float*)h->rho, (const float*)h->prs, h->ci,
-            h->consts, h->acc);
+  h->launch(K_FORCES, k_forces, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grid,
+            (const uint32_t*)h->keys, h->st[1], (const float4*)h->aux, h->ci, h->consts,
+            (const uint32_t*)h->nlist, (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
   if (until <= CLSPH_STAGE_FORCES) return 0;
   h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, 152 * 8)), dim3(kBlock), n, h->st[1],
             (const float4*)h->acc, h->st[0], h->mesh, h->consts, h->max_iters, h->bbox, h->status,
@@ -381,6 +395,9 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
     return fail(CLSPH_ERR_NO_DEVICE, "create: no CUDA device");
   clsph_gpu* h = new clsph_gpu();
   cudaGetDevice(&h->device);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) == cudaSuccess && sms > 0)
+    h->sm_count = (uint32_t)sms;
   h->n = n;
   h->params = *params;
   h->params.particles_count = n;
@@ -405,7 +422,9 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
   h->slots = slots;
   uint32_t log2s = 0;
   while ((1u << log2s) < slots) ++log2s;
-  if ((rc = dev_alloc(&h->rho, n)) || (rc = dev_alloc(&h->prs, n)) || (rc = dev_alloc(&h->acc, n)) ||
+  if ((rc = dev_alloc(&h->aux, n)) || (rc = dev_alloc(&h->acc, n)) ||
+      (rc = dev_alloc(&h->nlist, (size_t)h->nlist_cap * n)) || (rc = dev_alloc(&h->ncount, n)) ||
+      (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
       (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
       (rc = dev_alloc(&h->tile_hist, 256 * (size_t)h->ntiles)) ||
       (rc = dev_alloc(&h->digit_total, 4 * 256)) || (rc = dev_alloc(&h->ci.keys, slots)) ||
@@ -419,8 +438,8 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
   if (cudaMemset(h->grid, 0, sizeof(DevGrid)) != cudaSuccess ||
       cudaMemset(h->status, 0, sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(h->capped, 0, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(h->rho, 0, sizeof(float) * n) != cudaSuccess ||
-      cudaMemset(h->prs, 0, sizeof(float) * n) != cudaSuccess ||
+      cudaMemset(h->aux, 0, sizeof(float4) * n) != cudaSuccess ||
+      cudaMemset(h->ncount, 0, sizeof(uint32_t) * n) != cudaSuccess ||
       cudaMemset(h->acc, 0, sizeof(float4) * n) != cudaSuccess)
     return bail(fail(CLSPH_ERR_CUDA, "create: memset"));
   // identity ids
@@ -446,8 +465,11 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->st[s].ivel);
     cudaFree(h->ids[s]);
   }
-  cudaFree(h->rho);
-  cudaFree(h->prs);
+  cudaFree(h->aux);
+  cudaFree(h->nlist);
+  cudaFree(h->ncount);
+  cudaFree(h->cell_list);
+  cudaFree(h->step_counters);
   cudaFree(h->acc);
   cudaFree(h->keys);
   cudaFree(h->vals);
@@ -533,7 +555,7 @@ int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles) {
   if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "download: bad argument");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "download: no complete state");
   h->launch(K_PACK, k_pack_aos, dim3(grid_blocks(h->n, 152 * 8)), dim3(kBlock), h->aos_stage, h->n,
-            h->st[0], (const float*)h->rho, (const float*)h->prs, (const uint32_t*)h->keys,
+            h->st[0], (const float4*)h->aux, (const uint32_t*)h->keys,
             (const DevGrid*)h->grid, h->have_fields ? 1 : 0);
   CUDA_TRY(cudaMemcpyAsync(particles, h->aos_stage, sizeof(clsph_particle) * h->n,
                            cudaMemcpyDeviceToHost, h->stream));
@@ -625,8 +647,14 @@ int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap) {
 int clsph_gpu_read_fields(clsph_gpu* h, float* density, float* pressure, float* accel) {
   if (!h) return fail(CLSPH_ERR_ARGUMENT, "read_fields: null handle");
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  if (density) CUDA_TRY(cudaMemcpy(density, h->rho, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
-  if (pressure) CUDA_TRY(cudaMemcpy(pressure, h->prs, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
+  if (density || pressure) {
+    std::vector<float4> a(h->n);
+    CUDA_TRY(cudaMemcpy(a.data(), h->aux, sizeof(float4) * h->n, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < h->n; ++i) {
+      if (density) density[i] = a[i].x;
+      if (pressure) pressure[i] = a[i].y;
+    }
+  }
   if (accel) CUDA_TRY(cudaMemcpy(accel, h->acc, sizeof(float4) * h->n, cudaMemcpyDeviceToHost));
   return CLSPH_OK;
 }

@@ -2,7 +2,8 @@
 //
 // Data layout in HBM (SoA, sorted order, 16-byte float4 rows):
 //   pos[n], vel[n], ivel[n]   position, velocity, intermediate (half-step) velocity
-//   rho[n], prs[n]            density and Tait pressure of the substep
+//   aux[n]                    (rho, p, m/rho, p/rho^2) of the substep
+//   nlist[cap][n], ncount[n]  contributing neighbours of each particle, in visiting order
 //   acc[n]                    acceleration (forces -> advection)
 //   keys[2][n], vals[2][n]    radix-sort ping-pong (Morton key, source slot)
 //   ids[2][n]                 persistent particle ids (the reference has none)
@@ -23,6 +24,10 @@ constexpr int kRadixTile = kRadixThreads * kRadixItems;  // 4096 keys per tile
 constexpr int kRadixWarps = kRadixThreads / 32;
 constexpr int kRadixWarpSpan = kRadixTile / kRadixWarps;  // 512 keys per warp
 
+// per-substep counters, zeroed by k_grid_setup
+constexpr int kStepCounters = 8;
+enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntWorkForces = 2 };
+
 enum : uint32_t {
   kFlagGridOverflow = 1u,
   kFlagCollisionCap = 2u,
@@ -36,7 +41,8 @@ struct DevGrid {
   int32_t size[3];      // grid_size_x/y/z
   uint32_t cells;       // grid_cell_count (dense Morton range)
   uint32_t maxkey;      // largest key of the substep (sets the radix passes)
-  uint32_t pad_[4];
+  float half_margin;    // rounding margin of the half-cell tests, in cells
+  uint32_t pad_[3];
 };
 
 // 8-bit radix passes that cover every key of the substep.
@@ -114,26 +120,39 @@ __device__ __forceinline__ uint2 cell_lookup(const CellIndex& ci, uint32_t key) 
 
 // ---------------------------------------------------- neighbour cell window
 // The support radius is h but cells are 2h wide (grid.cl:56-61 vs
-// smoothing.cl:2), so along each axis only the neighbour cell on the side of
-// the particle's half of its own cell can hold particles within h. Cells
-// outside that window contribute exact zeros in the reference, so skipping
-// them keeps the reference's summation sequence. Particles within 1/256 of a
-// cell's middle keep all three cells (margin >> float rounding of t).
+// smoothing.cl:2). Each particle carries, per axis, whether it may lie in the
+// lower half of its cell (bit 2a) and whether it may lie in the upper half
+// (bit 2a+1), decided with a rounding margin so that a particle near the
+// middle has both bits. A particle with only the lower bit cannot be within
+// h of anything in the next cell up (the distance is > half a cell = h), and
+// symmetrically; cells and particles so excluded contribute exact zeros in
+// the reference, so skipping them keeps the reference's summation sequence.
+// The code is computed after the sort and kept in pos.w of the sorted state.
+__device__ __forceinline__ uint32_t half_code(float4 p, uint32_t key, const DevGrid& g) {
+  const uint32_t c[3] = {compact_bits3(key), compact_bits3(key >> 1), compact_bits3(key >> 2)};
+  const float pc[3] = {p.x, p.y, p.z};
+  uint32_t code = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float frac = XDIV(XSUB(pc[a], g.lo[a]), g.cell) - (float)c[a];
+    code |= (frac < 0.5f + g.half_margin ? 1u : 0u) << (2 * a);
+    code |= (frac > 0.5f - g.half_margin ? 1u : 0u) << (2 * a + 1);
+  }
+  return code;
+}
+
 struct Window {
   uint32_t lo[3], hi[3];
 };
 
 __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const DevGrid& g) {
   const uint32_t c[3] = {compact_bits3(key), compact_bits3(key >> 1), compact_bits3(key >> 2)};
-  const float pc[3] = {p.x, p.y, p.z};
+  const uint32_t code = __float_as_uint(p.w);
   Window w;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float t = XDIV(XSUB(pc[a], g.lo[a]), g.cell);
-    float frac = t - (float)c[a];
-    const float eps = 1.0f / 256.0f;
-    w.lo[a] = (frac < 0.5f + eps) ? c[a] - 1u : c[a];
-    w.hi[a] = (frac > 0.5f - eps) ? c[a] + 1u : c[a];
+    w.lo[a] = ((code >> (2 * a)) & 1u) ? c[a] - 1u : c[a];
+    w.hi[a] = ((code >> (2 * a + 1)) & 1u) ? c[a] + 1u : c[a];
   }
   return w;
 }
@@ -144,8 +163,10 @@ __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const
 // box accumulated by the previous kernel; resets the box and the radix digit
 // totals for this substep.
 __global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ grid, float h,
-                             uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total) {
+                             uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
+                             uint32_t* __restrict__ step_counters) {
   for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) digit_total[i] = 0u;
+  if (threadIdx.x < kStepCounters) step_counters[threadIdx.x] = 0u;
   if (threadIdx.x != 0) return;
   const float cell = XMUL(h, 2.f);
   DevGrid g;
@@ -164,7 +185,12 @@ __global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ 
   g.cell = cell;
   g.cells = morton3((uint32_t)g.size[0], (uint32_t)g.size[1], (uint32_t)g.size[2]);
   g.maxkey = 0u;
-  for (int i = 0; i < 4; ++i) g.pad_[i] = 0u;
+  // The cell coordinate t = fl(fl(p - lo) / 2h) is within ~2^-22 * t of the
+  // exact value and t < grid size G, so 2^-20 * (G + 2) covers its rounding
+  // and that of the distance test twice over.
+  const int gmax = max(g.size[0], max(g.size[1], g.size[2]));
+  g.half_margin = (float)(gmax + 2) * 0x1p-20f;
+  for (int i = 0; i < 3; ++i) g.pad_[i] = 0u;
   *grid = g;
   if (overflow) atomicOr(status, kFlagGridOverflow);
   // sentinels of sph_simulation.cpp:258-259 for the next accumulation
@@ -241,9 +267,8 @@ __global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State s
 
 // SoA -> host AoS: acceleration is 0 after the advection loop (sph.cl:97-99).
 __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
-                           const float* __restrict__ rho, const float* __restrict__ prs,
-                           const uint32_t* __restrict__ keys_base, const DevGrid* __restrict__ grid,
-                           int have_fields) {
+                           const float4* __restrict__ aux, const uint32_t* __restrict__ keys_base,
+                           const DevGrid* __restrict__ grid, int have_fields) {
   const uint32_t sel = have_fields ? sorted_sel(*grid) : 0u;
   const uint32_t* keys = keys_base + (size_t)sel * n;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -253,8 +278,9 @@ __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
     p[2] = st.ivel[i];
     p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 tail;
-    tail.x = have_fields ? rho[i] : 0.f;
-    tail.y = have_fields ? prs[i] : 0.f;
+    const float4 a = have_fields ? aux[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    tail.x = a.x;
+    tail.y = a.y;
     tail.z = __uint_as_float(have_fields ? keys[i] : 0u);
     tail.w = 0.f;
     p[4] = tail;
@@ -417,21 +443,25 @@ __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grid,
                          const uint32_t* __restrict__ keys_base,
                          const uint32_t* __restrict__ vals_base, State src, State dst,
                          const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
-                         CellIndex ci) {
+                         CellIndex ci, uint32_t* __restrict__ cell_list,
+                         uint32_t* __restrict__ cell_count) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint32_t sel = sorted_sel(*grid);
   const uint32_t* keys = keys_base + (size_t)sel * n;
   const uint32_t* perm = vals_base + (size_t)sel * n;
   const uint32_t from = perm[s];
-  dst.pos[s] = src.pos[from];
+  const uint32_t key = keys[s];
+  float4 p = src.pos[from];
+  p.w = __uint_as_float(half_code(p, key, *grid));
+  dst.pos[s] = p;
   dst.vel[s] = src.vel[from];
   dst.ivel[s] = src.ivel[from];
   ids_dst[s] = ids_src[from];
-  const uint32_t key = keys[s];
   if (s == 0 || keys[s - 1] != key) {
     uint32_t slot = cell_slot_insert(ci, key);
     if (slot != 0xFFFFFFFFu) ci.start[slot] = s;
+    cell_list[atomicAdd(cell_count, 1u)] = s;
   }
   if (s + 1 == n || keys[s + 1] != key) {
     uint32_t slot = cell_slot_insert(ci, key);
@@ -439,113 +469,236 @@ __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grid,
   }
 }
 
-// Density (forces.cl:15-43) and Tait pressure (sph.cl:36-39).
-__global__ void __launch_bounds__(kBlock)
-    k_density(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
-              const float4* __restrict__ pos, CellIndex ci, Consts c, float* __restrict__ rho_out,
-              float* __restrict__ prs_out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const DevGrid g = *grid;
-  const uint32_t* keys = keys_base + (size_t)(sorted_sel(g)) * n;
-  const float4 pi = pos[i];
-  const Window w = neighbour_window(pi, keys[i], g);
-  const float hh = XMUL(c.h, c.h);
-  float rho = 0.f;
-  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
-    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
-      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
-        const uint2 r = cell_lookup(ci, morton3(x, y, z));
-        for (uint32_t j = r.x; j < r.y; ++j) {
-          const float4 pj = __ldg(&pos[j]);
-          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
-          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-          if (r2 > c.cull_r2) continue;
-          const float rr = xnorm(d);
-          if (!(XDIV(rr, c.h) < 1.f)) continue;  // outside support: exact zero
-          const float q = XSUB(hh, XMUL(rr, rr));
-          rho = XADD(rho, XMUL(c.mass, XMUL(c.poly6, XMUL(XMUL(q, q), q))));
-        }
-      }
-  rho_out[i] = rho;
+// ------------------------------------------------- density and forces
+// Both gathers visit neighbours in the reference's order (27 cells in z, y, x
+// order, each cell's particles in sorted order; only the window cells can
+// contribute, the others add exact zeros) and evaluate every contributing
+// pair with IEEE round-to-nearest operations in the reference's expression
+// order, so the sums are bit-identical to the reference's.
+//
+// A candidate j contributes iff fl(r/h) < 1 (the (1 - clamp(floor(r/h),0,1))
+// factor of smoothing.cl). For floats r >= 0 and h > 0 that is exactly r < h:
+// fl(r/h) < 1 iff r/h < 1 - 2^-25, i.e. r < h(1 - 2^-25), and no float lies in
+// [h(1 - 2^-25), h) because the float below h is at most h(1 - 2^-24).
+//
+// Per particle the density kernel also stores (rho, p, m/rho, p/rho^2) -- the
+// same IEEE quotients the reference forms per pair -- and the list of its
+// contributing neighbours in visiting order (column-major, nlist[k*n + i]),
+// which the forces kernel walks without a second search.
+
+constexpr int kGatherBlock = 128;
+
+// Tait pressure (sph.cl:36-39): K * (pown(rho / rho0, 7) - 1).
+__device__ __forceinline__ float tait_pressure(float rho, const Consts& c) {
   const float x = XDIV(rho, c.rho0);
   float p7 = x;
 #pragma unroll
   for (int k = 1; k < 7; ++k) p7 = XMUL(p7, x);
-  prs_out[i] = XMUL(c.K, XSUB(p7, 1.f));
+  return XMUL(c.K, XSUB(p7, 1.f));
 }
 
-// Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58).
-__global__ void __launch_bounds__(kBlock)
-    k_forces(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
-             State st, const float* __restrict__ rho, const float* __restrict__ prs, CellIndex ci,
-             Consts c, float4* __restrict__ acc_out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const DevGrid g = *grid;
-  const uint32_t* keys = keys_base + (size_t)(sorted_sel(g)) * n;
-  const float4 pi = st.pos[i];
-  const float4 vi = st.vel[i];
-  const float rho_i = rho[i];
-  const float own = XDIV(prs[i], XMUL(rho_i, rho_i));
-  const Window w = neighbour_window(pi, keys[i], g);
-  const float hh = XMUL(c.h, c.h);
-  const float lap_b = XMUL(3.f, hh);
-  V3 P = {0.f, 0.f, 0.f}, Vs = {0.f, 0.f, 0.f}, Nm = {0.f, 0.f, 0.f};
-  float lap = 0.f;
+__device__ __forceinline__ float4 density_aux(float rho, const Consts& c) {
+  const float p = tait_pressure(rho, c);
+  return make_float4(rho, p, XDIV(c.mass, rho), XDIV(p, XMUL(rho, rho)));
+}
+
+// m * W_poly6(r) for a contributing pair (forces.cl:33-36, smoothing.cl:1-4).
+__device__ __forceinline__ float poly6_term(float rr, float hh, const Consts& c) {
+  const float q = XSUB(hh, XMUL(rr, rr));
+  return XMUL(c.mass, XMUL(c.poly6, XMUL(XMUL(q, q), q)));
+}
+
+struct ForceSums {
+  V3 P, Vs, Nm;
+  float lap;
+};
+
+// One contributing pair of forces.cl:67-97. aux_j = (rho_j, p_j, m/rho_j, p_j/rho_j^2).
+__device__ __forceinline__ void force_pair(ForceSums& f, bool self, V3 d, float rr, float4 vi,
+                                           float4 vj, float4 aux_j, float own, float hh,
+                                           float lap_b, const Consts& c) {
+  const float mj = aux_j.z;
+  if (!self) {
+    const float coef = XMUL(XADD(aux_j.w, own), c.mass);
+    V3 sg;
+    if (XSUB(rr, 0.0000001f) < 0.f) {  // smoothing.cl:23-25
+      sg = {c.spiky_zero, c.spiky_zero, c.spiky_zero};
+    } else {
+      const float q = XSUB(c.h, rr);
+      const float q2 = XMUL(q, q);
+      sg = {XMUL(XMUL(c.spiky, XDIV(d.x, rr)), q2), XMUL(XMUL(c.spiky, XDIV(d.y, rr)), q2),
+            XMUL(XMUL(c.spiky, XDIV(d.z, rr)), q2)};
+    }
+    f.P.x = XADD(f.P.x, XMUL(coef, sg.x));
+    f.P.y = XADD(f.P.y, XMUL(coef, sg.y));
+    f.P.z = XADD(f.P.z, XMUL(coef, sg.z));
+    const float vl = XMUL(c.visc, XSUB(c.h, rr));
+    f.Vs.x = XADD(f.Vs.x, XMUL(XMUL(XSUB(vj.x, vi.x), mj), vl));
+    f.Vs.y = XADD(f.Vs.y, XMUL(XMUL(XSUB(vj.y, vi.y), mj), vl));
+    f.Vs.z = XADD(f.Vs.z, XMUL(XMUL(XSUB(vj.z, vi.z), mj), vl));
+  }
+  const float q = XSUB(hh, XMUL(rr, rr));
+  const float q2 = XMUL(q, q);
+  f.Nm.x = XADD(f.Nm.x, XMUL(mj, XMUL(XMUL(c.grad6, d.x), q2)));
+  f.Nm.y = XADD(f.Nm.y, XMUL(mj, XMUL(XMUL(c.grad6, d.y), q2)));
+  f.Nm.z = XADD(f.Nm.z, XMUL(mj, XMUL(XMUL(c.grad6, d.z), q2)));
+  f.lap = XADD(f.lap, XMUL(mj, XMUL(XMUL(c.lap6, q), XSUB(lap_b, XMUL(7.f, XMUL(rr, rr))))));
+}
+
+// forces.cl:103-109 then sph.cl:53-58.
+__device__ __forceinline__ float4 finish_accel(const ForceSums& f, float rho_i, const Consts& c) {
+  const float nr = -rho_i;
+  V3 sum = {XADD(XMUL(nr, f.P.x), XMUL(f.Vs.x, c.mu)), XADD(XMUL(nr, f.P.y), XMUL(f.Vs.y, c.mu)),
+            XADD(XMUL(nr, f.P.z), XMUL(f.Vs.z, c.mu))};
+  const float nl = xnorm(f.Nm);
+  if (nl > c.sigma_threshold) {
+    const float s = XMUL(-c.sigma, f.lap);
+    sum.x = XADD(sum.x, XDIV(XMUL(s, f.Nm.x), nl));
+    sum.y = XADD(sum.y, XDIV(XMUL(s, f.Nm.y), nl));
+    sum.z = XADD(sum.z, XDIV(XMUL(s, f.Nm.z), nl));
+  }
+  return make_float4(XADD(XDIV(sum.x, rho_i), c.gx), XADD(XDIV(sum.y, rho_i), c.gy),
+                     XADD(XDIV(sum.z, rho_i), c.gz), 0.f);
+}
+
+// Calls f(j) for every candidate of particle i's window in the reference's order.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const Window& w, const CellIndex& ci, F&& f) {
   for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
     for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
       for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
         const uint2 r = cell_lookup(ci, morton3(x, y, z));
+        for (uint32_t j = r.x; j < r.y; ++j) f(j);
+      }
+}
+
+// Density (forces.cl:15-43) + Tait pressure (sph.cl:36-39) + neighbour list.
+// One thread per particle, two phases:
+//  1. walk the window cells (z, y, x order; each cell's particles in sorted
+//     order). A particle in a neighbour cell that lies in the half facing
+//     away from this particle's cell (per its half code in pos.w) is more
+//     than h away: skipped with one bit test. The others get an FMA distance
+//     cull; survivors are buffered per thread in shared memory;
+//  2. evaluate the survivors with exact arithmetic, in the same order, in
+//     lock-step across the warp (the expensive part is no longer divergent).
+// A thread with more survivors than its buffer repeats phase 1 inline.
+constexpr int kScanCap = 48;
+
+// Bits of a neighbour's half code that must be set for it to face cell
+// offset (ox, oy, oz): its upper half when it is below, lower half when above.
+__device__ __forceinline__ uint32_t facing_mask(int ox, int oy, int oz) {
+  uint32_t m = 0;
+  if (ox < 0) m |= 2u;
+  if (ox > 0) m |= 1u;
+  if (oy < 0) m |= 8u;
+  if (oy > 0) m |= 4u;
+  if (oz < 0) m |= 32u;
+  if (oz > 0) m |= 16u;
+  return m;
+}
+
+template <class F>
+__device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint32_t key,
+                                                          const CellIndex& ci,
+                                                          const float4* __restrict__ pos, F&& f) {
+  const int c[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
+  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
+    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
+      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
+        const uint32_t need = facing_mask((int)x - c[0], (int)y - c[1], (int)z - c[2]);
+        const uint2 r = cell_lookup(ci, morton3(x, y, z));
         for (uint32_t j = r.x; j < r.y; ++j) {
-          const float4 pj = __ldg(&st.pos[j]);
-          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
-          const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-          if (r2 > c.cull_r2) continue;
-          const float rr = xnorm(d);
-          if (!(XDIV(rr, c.h) < 1.f)) continue;  // every term is an exact zero
-          const float rho_j = __ldg(&rho[j]);
-          const float mj = XDIV(c.mass, rho_j);
-          if (j != i) {
-            const float coef = XMUL(XADD(XDIV(__ldg(&prs[j]), XMUL(rho_j, rho_j)), own), c.mass);
-            V3 sg;
-            if (XSUB(rr, 0.0000001f) < 0.f) {  // smoothing.cl:23-25
-              sg = {c.spiky_zero, c.spiky_zero, c.spiky_zero};
-            } else {
-              const float q = XSUB(c.h, rr);
-              const float q2 = XMUL(q, q);
-              sg = {XMUL(XMUL(c.spiky, XDIV(d.x, rr)), q2), XMUL(XMUL(c.spiky, XDIV(d.y, rr)), q2),
-                    XMUL(XMUL(c.spiky, XDIV(d.z, rr)), q2)};
-            }
-            P.x = XADD(P.x, XMUL(coef, sg.x));
-            P.y = XADD(P.y, XMUL(coef, sg.y));
-            P.z = XADD(P.z, XMUL(coef, sg.z));
-            const float vl = XMUL(c.visc, XSUB(c.h, rr));
-            const float4 vj = __ldg(&st.vel[j]);
-            Vs.x = XADD(Vs.x, XMUL(XMUL(XSUB(vj.x, vi.x), mj), vl));
-            Vs.y = XADD(Vs.y, XMUL(XMUL(XSUB(vj.y, vi.y), mj), vl));
-            Vs.z = XADD(Vs.z, XMUL(XMUL(XSUB(vj.z, vi.z), mj), vl));
-          }
-          const float q = XSUB(hh, XMUL(rr, rr));
-          const float q2 = XMUL(q, q);
-          Nm.x = XADD(Nm.x, XMUL(mj, XMUL(XMUL(c.grad6, d.x), q2)));
-          Nm.y = XADD(Nm.y, XMUL(mj, XMUL(XMUL(c.grad6, d.y), q2)));
-          Nm.z = XADD(Nm.z, XMUL(mj, XMUL(XMUL(c.grad6, d.z), q2)));
-          lap = XADD(lap, XMUL(mj, XMUL(XMUL(c.lap6, q), XSUB(lap_b, XMUL(7.f, XMUL(rr, rr))))));
+          const float4 pj = __ldg(&pos[j]);
+          if ((__float_as_uint(pj.w) & need) == need) f(j, pj);
         }
       }
-  const float nr = -rho_i;
-  V3 sum = {XADD(XMUL(nr, P.x), XMUL(Vs.x, c.mu)), XADD(XMUL(nr, P.y), XMUL(Vs.y, c.mu)),
-            XADD(XMUL(nr, P.z), XMUL(Vs.z, c.mu))};
-  const float nl = xnorm(Nm);
-  if (nl > c.sigma_threshold) {
-    const float s = XMUL(-c.sigma, lap);
-    sum.x = XADD(sum.x, XDIV(XMUL(s, Nm.x), nl));
-    sum.y = XADD(sum.y, XDIV(XMUL(s, Nm.y), nl));
-    sum.z = XADD(sum.z, XDIV(XMUL(s, Nm.z), nl));
+}
+
+__global__ void __launch_bounds__(kGatherBlock)
+    k_density(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
+              const float4* __restrict__ pos, CellIndex ci, Consts c, float4* __restrict__ aux_out,
+              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap) {
+  __shared__ uint32_t cand[kScanCap][kGatherBlock];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DevGrid g = *grid;
+  const uint32_t* keys = keys_base + (size_t)sorted_sel(g) * n;
+  const uint32_t key = keys[i];
+  const float4 pi = pos[i];
+  const Window w = neighbour_window(pi, key, g);
+  const float hh = XMUL(c.h, c.h);
+  uint32_t found = 0;
+  for_each_facing_candidate(w, key, ci, pos, [&](uint32_t j, float4 pj) {
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) {
+      if (found < kScanCap) cand[found][threadIdx.x] = j;
+      ++found;
+    }
+  });
+  float rho = 0.f;
+  uint32_t kept = 0;
+  auto visit = [&](uint32_t j, float4 pj) {
+    const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+    const float rr = xnorm(d);
+    if (rr < c.h) {
+      rho = XADD(rho, poly6_term(rr, hh, c));
+      if (kept < nlist_cap) nlist[(size_t)kept * n + i] = j;
+      ++kept;
+    }
+  };
+  if (found <= (uint32_t)kScanCap) {
+    for (uint32_t k = 0; k < found; ++k) {
+      const uint32_t j = cand[k][threadIdx.x];
+      visit(j, __ldg(&pos[j]));
+    }
+  } else {
+    for_each_facing_candidate(w, key, ci, pos, [&](uint32_t j, float4 pj) {
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj);
+    });
   }
-  acc_out[i] = make_float4(XADD(XDIV(sum.x, rho_i), c.gx), XADD(XDIV(sum.y, rho_i), c.gy),
-                           XADD(XDIV(sum.z, rho_i), c.gz), 0.f);
+  aux_out[i] = density_aux(rho, c);
+  ncount[i] = kept;  // > nlist_cap: the list is incomplete, forces search again
+}
+
+// Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58), walking
+// the neighbour list of k_density (or the window, for overflowing lists).
+__global__ void __launch_bounds__(kGatherBlock)
+    k_forces(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
+             State st, const float4* __restrict__ aux, CellIndex ci, Consts c,
+             const uint32_t* __restrict__ nlist, const uint32_t* __restrict__ ncount,
+             uint32_t nlist_cap, float4* __restrict__ acc_out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 pi = st.pos[i];
+  const float4 vi = st.vel[i];
+  const float4 ai = aux[i];
+  const float own = ai.w;
+  const float hh = XMUL(c.h, c.h);
+  const float lap_b = XMUL(3.f, hh);
+  ForceSums f = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
+  auto pair = [&](uint32_t j) {
+    const float4 pj = __ldg(&st.pos[j]);
+    const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+    const float rr = xnorm(d);
+    force_pair(f, j == i, d, rr, vi, __ldg(&st.vel[j]), __ldg(&aux[j]), own, hh, lap_b, c);
+  };
+  const uint32_t cnt = ncount[i];
+  if (cnt <= nlist_cap) {
+    for (uint32_t k = 0; k < cnt; ++k) pair(__ldg(&nlist[(size_t)k * n + i]));
+  } else {
+    const DevGrid g = *grid;
+    const uint32_t* keys = keys_base + (size_t)sorted_sel(g) * n;
+    const Window w = neighbour_window(pi, keys[i], g);
+    for_each_candidate(w, ci, [&](uint32_t j) {
+      const float4 pj = __ldg(&st.pos[j]);
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > c.cull_r2) return;
+      const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+      if (xnorm(d) < c.h) pair(j);
+    });
+  }
+  acc_out[i] = finish_accel(f, ai.x, c);
 }
 
 // ------------------------------------------------------- mesh collision
