@@ -88,6 +88,16 @@ enum {
  * (sph_simulation.cpp:459-559); particles_count is replaced by n. */
 int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
                      clsph_gpu** out);
+
+/* S independent scenes in one handle (no counterpart in the reference, which
+ * runs one scene per sph_simulation): params[s], terms[s] and counts[s] are
+ * scene s's derived parameter block, kernel constants and particle count.
+ * Every substep runs all scenes in the same kernel launches; scene s's
+ * particles are slots [sum(counts[<s]), sum(counts[<=s])) of the AoS given to
+ * upload/download, and each scene's result is the one a handle of its own
+ * would produce (own grid, own sort order, own mesh). S <= 65535. */
+int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_terms* terms,
+                             const uint32_t* counts, uint32_t nscenes, clsph_gpu** out);
 int clsph_gpu_destroy(clsph_gpu* h);
 
 /* Cap of the advect/collide loop per particle and substep (default 1024).
@@ -105,6 +115,16 @@ int clsph_gpu_set_stream(clsph_gpu* h, void* cuda_stream);
  * brute-force loop (collisions.cl:21-87). */
 int clsph_gpu_set_mesh(clsph_gpu* h, const float* face_normals, const float* vertices,
                        uint32_t vertex_count, const uint32_t* indices, uint32_t face_count);
+/* The mesh of one scene of a batched handle (clsph_gpu_set_mesh = scene 0). */
+int clsph_gpu_set_scene_mesh(clsph_gpu* h, uint32_t scene, const float* face_normals,
+                             const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                             uint32_t face_count);
+
+/* Replay substeps from a CUDA graph of two captured substeps (1) or launch
+ * every kernel (0, default). The graph is captured on the first clsph_gpu_step
+ * of at least two substeps and re-captured when the collision cap changes;
+ * it is bypassed while profiling. */
+int clsph_gpu_set_graph(clsph_gpu* h, int enabled);
 
 /* Replaces the enqueueWriteBuffer of sph_simulation.cpp:249-251: host AoS ->
  * device. `particles` points to n clsph_particle (only position, velocity and
@@ -132,15 +152,19 @@ int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags);
 /* The parameter block with the grid of the last substep (min_point,
  * max_point, grid_size_*, grid_cell_count), as sph_simulation keeps it. */
 int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out);
+int clsph_gpu_get_scene_parameters(clsph_gpu* h, uint32_t scene, clsph_parameters* out);
 
-/* Inspection (synchronising). keys: sorted grid_index per slot; perm: sorted
- * slot -> slot before the sort (may be NULL). */
+/* Inspection (synchronising). keys: sorted grid_index (the scene's Morton
+ * key) per slot; perm: sorted slot -> slot before the sort (may be NULL). */
 int clsph_gpu_read_keys(clsph_gpu* h, uint32_t* keys, uint32_t* perm);
 
 /* The reference's dense cell table (sph_simulation.cpp:216-224) rebuilt from
  * the device cell index: table[c] = first sorted slot with key >= c, for
  * c < grid_cell_count. Needs cap >= grid_cell_count. Debug path: allocates. */
 int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap);
+/* The same for one scene of a batched handle: slots relative to the scene's
+ * first slot. */
+int clsph_gpu_read_cell_table_scene(clsph_gpu* h, uint32_t scene, uint32_t* table, uint64_t cap);
 
 /* density[n], pressure[n], accel[4n] (x, y, z, 0) of the last substep; any
  * pointer may be NULL. accel is valid after CLSPH_STAGE_FORCES. */

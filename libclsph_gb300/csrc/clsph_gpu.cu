@@ -1,13 +1,16 @@
 // C ABI of the GB300 SPH substep engine (include/clsph_gpu.h).
 //
-// One handle owns every device buffer for n particles (allocated once in
-// clsph_gpu_create), the scene mesh with its per-cell triangle lists, and a
-// stream. clsph_gpu_step enqueues the substep kernels of clsph_kernels.cuh;
-// no host round trip and no allocation happens between substeps.
+// One handle owns every device buffer for its particles (allocated once at
+// create), the scene meshes with their per-cell triangle lists, and a
+// stream. A handle runs S independent scenes (S = 1 for clsph_gpu_create):
+// every kernel of a substep covers all scenes in one launch.
+// clsph_gpu_step enqueues the substep kernels of clsph_kernels.cuh, replayed
+// from a CUDA graph when enabled; no host round trip and no allocation
+// happens between substeps.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
-#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -60,6 +63,9 @@ const char* kKernelNames[K_NUM_CLASSES] = {
     "grid_setup", "keys", "radix_count", "radix_scan", "radix_scatter", "gather",
     "density",    "forces", "advect",   "unpack_aos", "pack_aos",      "misc"};
 
+// kernels enqueued by one full substep (4 radix passes x 3 kernels)
+constexpr uint32_t kLaunchesPerSubstep = 2 + 12 + 4;
+
 struct PendingTiming {
   int cls;
   cudaEvent_t start, stop;
@@ -85,6 +91,23 @@ float pown_f(float x, int k) {
   return r;
 }
 
+// Device buffers of one scene's mesh.
+struct SceneMesh {
+  float* normals = nullptr;
+  float* vertices = nullptr;
+  uint32_t* indices = nullptr;
+  uint32_t* cell_start = nullptr;
+  uint32_t* cell_faces = nullptr;
+  void release() {
+    cudaFree(normals);
+    cudaFree(vertices);
+    cudaFree(indices);
+    cudaFree(cell_start);
+    cudaFree(cell_faces);
+    *this = SceneMesh{};
+  }
+};
+
 }  // namespace
 
 // Error text for clsph_gpu_last_error from the library's other translation units.
@@ -96,9 +119,22 @@ struct clsph_gpu {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   uint32_t n = 0;
-  clsph_parameters params{};
-  clsph_kernel_terms terms{};
-  Consts consts{};
+
+  // scenes
+  uint32_t nscenes = 1;
+  std::vector<uint32_t> scene_first;  // nscenes + 1 slot offsets
+  std::vector<clsph_parameters> params;
+  std::vector<clsph_kernel_terms> terms;
+  std::vector<Consts> consts_host;
+  std::vector<SceneMesh> scene_mesh;
+  std::vector<DevMesh> mesh_host;
+  uint16_t* scene_of = nullptr;
+  DevGrid* grids = nullptr;
+  Consts* consts = nullptr;
+  float* scene_h = nullptr;
+  DevMesh* meshes = nullptr;
+  uint32_t* bbox = nullptr;  // 6 per scene
+  uint32_t* ctl = nullptr;   // kCtlWords
 
   State st[2]{};
   uint32_t* ids[2]{};
@@ -107,34 +143,29 @@ struct clsph_gpu {
   float4* acc = nullptr;
   uint32_t* nlist = nullptr;
   uint32_t* ncount = nullptr;
+  uint32_t nlist_cap = 64;
   uint32_t* cell_list = nullptr;      // first sorted slot of every occupied cell
   uint32_t* step_counters = nullptr;  // kStepCounters, zeroed every substep
-  uint32_t nlist_cap = 64;
-  uint32_t* keys = nullptr;  // [2n]
-  uint32_t* vals = nullptr;  // [2n]
+  uint32_t* keys = nullptr;           // [2n]
+  uint32_t* vals = nullptr;           // [2n]
   uint32_t* tile_hist = nullptr;
   uint32_t ntiles = 0;
   uint32_t* digit_total = nullptr;
   CellIndex ci{};
   uint32_t slots = 0;
-  DevGrid* grid = nullptr;
-  uint32_t* bbox = nullptr;
   uint32_t* status = nullptr;
   unsigned long long* capped = nullptr;
   float4* aos_stage = nullptr;
-
-  // mesh
-  float* d_normals = nullptr;
-  float* d_vertices = nullptr;
-  uint32_t* d_indices = nullptr;
-  uint32_t* d_cell_start = nullptr;
-  uint32_t* d_cell_faces = nullptr;
-  DevMesh mesh{};
 
   bool uploaded = false;
   bool partial = false;
   bool have_fields = false;
   uint32_t max_iters = 1024;
+
+  // CUDA graphs of two substeps, one per buffer the particle ids start in
+  bool use_graph = false;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  uint32_t graph_max_iters[2] = {0, 0};
 
   bool profiling = false;
   std::vector<PendingTiming> pending;
@@ -157,17 +188,12 @@ struct clsph_gpu {
 
   template <typename Kernel, typename... Args>
   void launch(int cls, Kernel k, dim3 g, dim3 b, Args... args) {
-    launch_smem(cls, k, g, b, 0, args...);
-  }
-
-  template <typename Kernel, typename... Args>
-  void launch_smem(int cls, Kernel k, dim3 g, dim3 b, size_t smem, Args... args) {
     PendingTiming t{cls, nullptr, nullptr};
     if (profiling) {
       t.start = take_event();
       cudaEventRecord(t.start, stream);
     }
-    k<<<g, b, smem, stream>>>(args...);
+    k<<<g, b, 0, stream>>>(args...);
     ++launches;
     if (profiling) {
       t.stop = take_event();
@@ -189,25 +215,19 @@ struct clsph_gpu {
     pending.clear();
   }
 
-  void free_mesh() {
-    cudaFree(d_normals);
-    cudaFree(d_vertices);
-    cudaFree(d_indices);
-    cudaFree(d_cell_start);
-    cudaFree(d_cell_faces);
-    d_normals = d_vertices = nullptr;
-    d_indices = d_cell_start = d_cell_faces = nullptr;
-    mesh = DevMesh{};
+  void drop_graph() {
+    for (auto& g : graph_exec) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   }
 };
 
 namespace {
 
-void derive_consts(clsph_gpu* h) {
-  const clsph_parameters& p = h->params;
-  const clsph_kernel_terms& t = h->terms;
-  Consts& c = h->consts;
-  c.n = h->n;
+Consts derive_consts(const clsph_parameters& p, const clsph_kernel_terms& t, uint32_t n) {
+  Consts c{};
+  c.n = n;
   c.h = p.h;
   c.mass = p.particle_mass;
   c.rho0 = p.fluid_density;
@@ -230,45 +250,49 @@ void derive_consts(clsph_gpu* h) {
   // smoothing.cl:24: -45 / (float)(M_PI * pown(h, 6)) with M_PI in double
   c.spiky_zero = -45.f / (float)(M_PI * (double)pown_f(p.h, 6));
   c.cull_r2 = p.h * p.h * 1.0001f;
+  return c;
 }
 
 int enqueue_substep(clsph_gpu* h, int until) {
   const uint32_t n = h->n;
   const uint32_t blocks = grid_blocks(n);
-  h->launch(K_GRID_SETUP, k_grid_setup, dim3(1), dim3(256), h->bbox, h->grid, h->params.h,
-            h->status, h->digit_total, h->step_counters);
+  const uint32_t* cctl = h->ctl;
+  h->launch(K_GRID_SETUP, k_grid_setup, dim3(1), dim3(256), h->bbox, h->grids,
+            (const float*)h->scene_h, h->nscenes, h->status, h->digit_total, h->step_counters,
+            h->ctl);
   CUDA_TRY(cudaMemsetAsync(h->ci.keys, 0, sizeof(uint32_t) * h->slots, h->stream));
-  h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n, h->grid,
-            h->keys);
+  h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n,
+            (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, h->ctl, h->keys);
   if (until <= CLSPH_STAGE_GRID) return 0;
   for (int pass = 0; pass < 4; ++pass) {
     h->launch(K_RADIX_COUNT, k_radix_count, dim3(h->ntiles), dim3(kRadixThreads),
-              (const uint32_t*)h->keys, n, pass, (const DevGrid*)h->grid, h->tile_hist, h->ntiles,
-              h->digit_total);
+              (const uint32_t*)h->keys, n, pass, cctl, h->tile_hist, h->ntiles, h->digit_total);
     h->launch(K_RADIX_SCAN, k_radix_scan, dim3(256), dim3(kRadixThreads), h->tile_hist, h->ntiles,
-              pass, (const DevGrid*)h->grid, (const uint32_t*)h->digit_total);
+              pass, cctl, (const uint32_t*)h->digit_total);
     h->launch(K_RADIX_SCATTER, k_radix_scatter, dim3(h->ntiles), dim3(kRadixThreads), h->keys,
-              h->vals, n, pass, (const DevGrid*)h->grid, (const uint32_t*)h->tile_hist, h->ntiles);
+              h->vals, n, pass, cctl, (const uint32_t*)h->tile_hist, h->ntiles);
   }
   const int src_ids = h->ids_sel, dst_ids = h->ids_sel ^ 1;
-  h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grid,
-            (const uint32_t*)h->keys, (const uint32_t*)h->vals, h->st[0], h->st[1],
-            (const uint32_t*)h->ids[src_ids], h->ids[dst_ids], h->ci, h->cell_list,
-            h->step_counters + kCntCells);
+  h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grids,
+            (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
+            (const uint32_t*)h->vals, h->st[0], h->st[1], (const uint32_t*)h->ids[src_ids],
+            h->ids[dst_ids], h->ci, h->cell_list, h->step_counters + kCntCells);
   h->ids_sel = dst_ids;
   if (until <= CLSPH_STAGE_SORT) return 0;
   const uint32_t gblocks = (n + kGatherBlock - 1) / kGatherBlock;
-  h->launch(K_DENSITY, k_density, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grid,
-            (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci, h->consts, h->aux,
-            h->nlist, h->ncount, h->nlist_cap);
+  h->launch(K_DENSITY, k_density, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grids,
+            (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
+            (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
+            h->ncount, h->nlist_cap);
   if (until <= CLSPH_STAGE_DENSITY) return 0;
-  h->launch(K_FORCES, k_forces, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grid,
-            (const uint32_t*)h->keys, h->st[1], (const float4*)h->aux, h->ci, h->consts,
-            (const uint32_t*)h->nlist, (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
+  h->launch(K_FORCES, k_forces, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grids,
+            (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
+            (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
+            (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
   if (until <= CLSPH_STAGE_FORCES) return 0;
-  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, 152 * 8)), dim3(kBlock), n, h->st[1],
-            (const float4*)h->acc, h->st[0], h->mesh, h->consts, h->max_iters, h->bbox, h->status,
-            h->capped);
+  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, h->sm_count * 8)), dim3(kBlock), n, h->st[1],
+            (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes, (const Consts*)h->consts,
+            (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status, h->capped);
   return 0;
 }
 
@@ -279,9 +303,40 @@ int check_launch(clsph_gpu* h) {
   return 0;
 }
 
-int read_grid(clsph_gpu* h, DevGrid* g) {
+// Two substeps captured once and replayed. The particle ids alternate between
+// their two buffers, so a pair returns them to the buffer it started from;
+// there is one graph per starting buffer.
+int ensure_graph(clsph_gpu* h) {
+  const int par = h->ids_sel;
+  if (h->graph_exec[par] && h->graph_max_iters[par] == h->max_iters) return 0;
+  if (h->graph_exec[par]) cudaGraphExecDestroy(h->graph_exec[par]);
+  h->graph_exec[par] = nullptr;
+  cudaGraph_t graph = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const uint64_t launches = h->launches;
+  int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+  if (!rc) rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+  h->launches = launches;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph_exec[par], graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    h->graph_exec[par] = nullptr;
+    return fail(CLSPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  h->graph_max_iters[par] = h->max_iters;
+  return 0;
+}
+
+int read_grid(clsph_gpu* h, uint32_t scene, DevGrid* g, uint32_t* ctl) {
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  CUDA_TRY(cudaMemcpy(g, h->grid, sizeof(DevGrid), cudaMemcpyDeviceToHost));
+  if (g) CUDA_TRY(cudaMemcpy(g, h->grids + scene, sizeof(DevGrid), cudaMemcpyDeviceToHost));
+  if (ctl) CUDA_TRY(cudaMemcpy(ctl, h->ctl, sizeof(uint32_t) * kCtlWords, cudaMemcpyDeviceToHost));
   return 0;
 }
 
@@ -290,8 +345,9 @@ int read_grid(clsph_gpu* h, DevGrid* g) {
 // cell is listed there in ascending face order, so scanning one list equals
 // the reference's scan over all faces for any segment that starts in the
 // cell and is no longer than the reach.
-int build_face_grid(clsph_gpu* h, const float* vx, uint32_t nv, const uint32_t* ix, uint32_t faces,
-                    std::vector<uint32_t>& start, std::vector<uint32_t>& list) {
+int build_face_grid(const clsph_parameters& p, const float* vx, uint32_t nv, const uint32_t* ix,
+                    uint32_t faces, std::vector<uint32_t>& start, std::vector<uint32_t>& list,
+                    DevMesh& mesh) {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (uint32_t f = 0; f < faces; ++f)
     for (int k = 0; k < 3; ++k) {
@@ -304,7 +360,6 @@ int build_face_grid(clsph_gpu* h, const float* vx, uint32_t nv, const uint32_t* 
         hi[a] = std::fmax(hi[a], c);
       }
     }
-  const clsph_parameters& p = h->params;
   float extent = 0.f;
   for (int a = 0; a < 3; ++a) extent = std::fmax(extent, hi[a] - lo[a]);
   const float reach = std::fmax(p.max_velocity * p.time_delta * p.simulation_scale * 1.5f + 0.002f, 1e-4f);
@@ -371,11 +426,17 @@ int build_face_grid(clsph_gpu* h, const float* vx, uint32_t nv, const uint32_t* 
     }
   }
   for (int a = 0; a < 3; ++a) {
-    h->mesh.lo[a] = glo[a];
-    h->mesh.dims[a] = dims[a];
+    mesh.lo[a] = glo[a];
+    mesh.dims[a] = dims[a];
   }
-  h->mesh.inv_cell = 1.f / cell;
-  h->mesh.reach = reach;
+  mesh.inv_cell = 1.f / cell;
+  mesh.reach = reach;
+  return 0;
+}
+
+int sync_scene_tables(clsph_gpu* h) {
+  CUDA_TRY(cudaMemcpy(h->consts, h->consts_host.data(), sizeof(Consts) * h->nscenes, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->meshes, h->mesh_host.data(), sizeof(DevMesh) * h->nscenes, cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -385,11 +446,20 @@ extern "C" {
 
 const char* clsph_gpu_last_error(void) { return g_last_error.c_str(); }
 
-int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
-                     clsph_gpu** out) {
-  if (!params || !terms || !out || n == 0) return fail(CLSPH_ERR_ARGUMENT, "create: bad argument");
-  if (n > (1u << 28)) return fail(CLSPH_ERR_TOO_LARGE, "create: more than 2^28 particles");
-  if (!(params->h > 0.f)) return fail(CLSPH_ERR_ARGUMENT, "create: h must be positive");
+int clsph_gpu_destroy(clsph_gpu* h);
+
+int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_terms* terms,
+                             const uint32_t* counts, uint32_t nscenes, clsph_gpu** out) {
+  if (!params || !terms || !counts || !out || nscenes == 0)
+    return fail(CLSPH_ERR_ARGUMENT, "create: bad argument");
+  if (nscenes > 65535) return fail(CLSPH_ERR_TOO_LARGE, "create: more than 65535 scenes");
+  uint64_t total = 0;
+  for (uint32_t s = 0; s < nscenes; ++s) {
+    if (counts[s] == 0) return fail(CLSPH_ERR_ARGUMENT, "create: a scene has no particles");
+    if (!(params[s].h > 0.f)) return fail(CLSPH_ERR_ARGUMENT, "create: h must be positive");
+    total += counts[s];
+  }
+  if (total > (1u << 28)) return fail(CLSPH_ERR_TOO_LARGE, "create: more than 2^28 particles");
   int devices = 0;
   if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
     return fail(CLSPH_ERR_NO_DEVICE, "create: no CUDA device");
@@ -398,11 +468,20 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) == cudaSuccess && sms > 0)
     h->sm_count = (uint32_t)sms;
+  const uint32_t n = (uint32_t)total;
   h->n = n;
-  h->params = *params;
-  h->params.particles_count = n;
-  h->terms = *terms;
-  derive_consts(h);
+  h->nscenes = nscenes;
+  h->scene_first.assign(nscenes + 1, 0u);
+  for (uint32_t s = 0; s < nscenes; ++s) {
+    h->scene_first[s + 1] = h->scene_first[s] + counts[s];
+    clsph_parameters p = params[s];
+    p.particles_count = counts[s];
+    h->params.push_back(p);
+    h->terms.push_back(terms[s]);
+    h->consts_host.push_back(derive_consts(p, terms[s], counts[s]));
+  }
+  h->scene_mesh.resize(nscenes);
+  h->mesh_host.assign(nscenes, DevMesh{});
   int rc = 0;
   auto bail = [&](int code) {
     clsph_gpu_destroy(h);
@@ -429,31 +508,53 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
       (rc = dev_alloc(&h->tile_hist, 256 * (size_t)h->ntiles)) ||
       (rc = dev_alloc(&h->digit_total, 4 * 256)) || (rc = dev_alloc(&h->ci.keys, slots)) ||
       (rc = dev_alloc(&h->ci.start, slots)) || (rc = dev_alloc(&h->ci.end, slots)) ||
-      (rc = dev_alloc(&h->grid, 1)) || (rc = dev_alloc(&h->bbox, 6)) ||
-      (rc = dev_alloc(&h->status, 1)) || (rc = dev_alloc(&h->capped, 1)) ||
-      (rc = dev_alloc(&h->aos_stage, 5 * (size_t)n)))
+      (rc = dev_alloc(&h->scene_of, n)) || (rc = dev_alloc(&h->grids, nscenes)) ||
+      (rc = dev_alloc(&h->consts, nscenes)) || (rc = dev_alloc(&h->scene_h, nscenes)) ||
+      (rc = dev_alloc(&h->meshes, nscenes)) || (rc = dev_alloc(&h->bbox, 6 * (size_t)nscenes)) ||
+      (rc = dev_alloc(&h->ctl, kCtlWords)) || (rc = dev_alloc(&h->status, 1)) ||
+      (rc = dev_alloc(&h->capped, 1)) || (rc = dev_alloc(&h->aos_stage, 5 * (size_t)n)))
     return bail(rc);
   h->ci.mask = slots - 1;
   h->ci.shift = 32 - log2s;
-  if (cudaMemset(h->grid, 0, sizeof(DevGrid)) != cudaSuccess ||
+  uint32_t scene_bits = 0;
+  while ((1u << scene_bits) < nscenes) ++scene_bits;
+  uint32_t ctl_init[kCtlWords] = {};
+  ctl_init[kCtlSceneBits] = scene_bits;
+  ctl_init[kCtlShift] = 1;
+  std::vector<uint16_t> scene_of(n);
+  std::vector<float> hs(nscenes);
+  for (uint32_t s = 0; s < nscenes; ++s) {
+    hs[s] = h->params[s].h;
+    for (uint32_t i = h->scene_first[s]; i < h->scene_first[s + 1]; ++i) scene_of[i] = (uint16_t)s;
+  }
+  std::vector<uint32_t> iota(n);
+  for (uint32_t i = 0; i < n; ++i) iota[i] = i;
+  if (cudaMemset(h->grids, 0, sizeof(DevGrid) * nscenes) != cudaSuccess ||
       cudaMemset(h->status, 0, sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(h->capped, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemset(h->aux, 0, sizeof(float4) * n) != cudaSuccess ||
       cudaMemset(h->ncount, 0, sizeof(uint32_t) * n) != cudaSuccess ||
-      cudaMemset(h->acc, 0, sizeof(float4) * n) != cudaSuccess)
-    return bail(fail(CLSPH_ERR_CUDA, "create: memset"));
-  // identity ids
-  std::vector<uint32_t> iota(n);
-  for (uint32_t i = 0; i < n; ++i) iota[i] = i;
-  if (cudaMemcpy(h->ids[0], iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess)
-    return bail(fail(CLSPH_ERR_CUDA, "create: ids"));
+      cudaMemset(h->acc, 0, sizeof(float4) * n) != cudaSuccess ||
+      cudaMemcpy(h->ctl, ctl_init, sizeof(ctl_init), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->scene_of, scene_of.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->scene_h, hs.data(), sizeof(float) * nscenes, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->ids[0], iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "create: initialisation copies"));
+  if ((rc = sync_scene_tables(h))) return bail(rc);
   *out = h;
   return CLSPH_OK;
+}
+
+int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
+                     clsph_gpu** out) {
+  if (!params || !terms || !out || n == 0) return fail(CLSPH_ERR_ARGUMENT, "create: bad argument");
+  return clsph_gpu_create_batched(params, terms, &n, 1, out);
 }
 
 int clsph_gpu_destroy(clsph_gpu* h) {
   if (!h) return CLSPH_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  h->drop_graph();
   for (auto& t : h->pending) {
     cudaEventDestroy(t.start);
     cudaEventDestroy(t.stop);
@@ -465,25 +566,13 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->st[s].ivel);
     cudaFree(h->ids[s]);
   }
-  cudaFree(h->aux);
-  cudaFree(h->nlist);
-  cudaFree(h->ncount);
-  cudaFree(h->cell_list);
-  cudaFree(h->step_counters);
-  cudaFree(h->acc);
-  cudaFree(h->keys);
-  cudaFree(h->vals);
-  cudaFree(h->tile_hist);
-  cudaFree(h->digit_total);
-  cudaFree(h->ci.keys);
-  cudaFree(h->ci.start);
-  cudaFree(h->ci.end);
-  cudaFree(h->grid);
-  cudaFree(h->bbox);
-  cudaFree(h->status);
-  cudaFree(h->capped);
-  cudaFree(h->aos_stage);
-  h->free_mesh();
+  void* bufs[] = {h->aux,      h->acc,      h->nlist,     h->ncount,      h->cell_list,
+                  h->step_counters, h->keys, h->vals,     h->tile_hist,   h->digit_total,
+                  h->ci.keys,  h->ci.start, h->ci.end,    h->scene_of,    h->grids,
+                  h->consts,   h->scene_h,  h->meshes,    h->bbox,        h->ctl,
+                  h->status,   h->capped,   h->aos_stage};
+  for (void* b : bufs) cudaFree(b);
+  for (auto& m : h->scene_mesh) m.release();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return CLSPH_OK;
@@ -502,49 +591,69 @@ int clsph_gpu_set_stream(clsph_gpu* h, void* stream) {
   return CLSPH_OK;
 }
 
-int clsph_gpu_set_mesh(clsph_gpu* h, const float* normals, const float* vertices,
-                       uint32_t vertex_count, const uint32_t* indices, uint32_t faces) {
-  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_mesh: null handle");
+int clsph_gpu_set_graph(clsph_gpu* h, int enabled) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_graph: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->use_graph = enabled != 0;
+  if (!h->use_graph) h->drop_graph();
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_scene_mesh(clsph_gpu* h, uint32_t scene, const float* normals,
+                             const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                             uint32_t faces) {
+  if (!h || scene >= h->nscenes) return fail(CLSPH_ERR_ARGUMENT, "set_mesh: bad handle or scene");
   if (faces && (!normals || !vertices || !indices))
     return fail(CLSPH_ERR_ARGUMENT, "set_mesh: null mesh array");
   for (uint64_t k = 0; k < 3ull * faces; ++k)
     if (indices[k] >= vertex_count) return fail(CLSPH_ERR_ARGUMENT, "set_mesh: vertex index out of range");
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  h->free_mesh();
-  if (faces == 0) return CLSPH_OK;
-  int rc;
-  if ((rc = dev_alloc(&h->d_normals, 3 * (size_t)faces)) ||
-      (rc = dev_alloc(&h->d_vertices, 3 * (size_t)vertex_count)) ||
-      (rc = dev_alloc(&h->d_indices, 3 * (size_t)faces)))
-    return rc;
-  CUDA_TRY(cudaMemcpy(h->d_normals, normals, sizeof(float) * 3 * faces, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(h->d_vertices, vertices, sizeof(float) * 3 * vertex_count, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(h->d_indices, indices, sizeof(uint32_t) * 3 * faces, cudaMemcpyHostToDevice));
-  h->mesh.normals = h->d_normals;
-  h->mesh.vertices = h->d_vertices;
-  h->mesh.indices = h->d_indices;
-  h->mesh.faces = faces;
-  std::vector<uint32_t> start, list;
-  rc = build_face_grid(h, vertices, vertex_count, indices, faces, start, list);
-  if (rc >= 256) return rc;
-  if (rc == 0) {
-    if ((rc = dev_alloc(&h->d_cell_start, start.size())) || (rc = dev_alloc(&h->d_cell_faces, list.size())))
+  SceneMesh& sm = h->scene_mesh[scene];
+  DevMesh& dm = h->mesh_host[scene];
+  sm.release();
+  dm = DevMesh{};
+  if (faces) {
+    int rc;
+    if ((rc = dev_alloc(&sm.normals, 3 * (size_t)faces)) ||
+        (rc = dev_alloc(&sm.vertices, 3 * (size_t)vertex_count)) ||
+        (rc = dev_alloc(&sm.indices, 3 * (size_t)faces)))
       return rc;
-    CUDA_TRY(cudaMemcpy(h->d_cell_start, start.data(), sizeof(uint32_t) * start.size(), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(h->d_cell_faces, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice));
-    h->mesh.cell_start = h->d_cell_start;
-    h->mesh.cell_faces = h->d_cell_faces;
+    CUDA_TRY(cudaMemcpy(sm.normals, normals, sizeof(float) * 3 * faces, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(sm.vertices, vertices, sizeof(float) * 3 * vertex_count, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(sm.indices, indices, sizeof(uint32_t) * 3 * faces, cudaMemcpyHostToDevice));
+    dm.normals = sm.normals;
+    dm.vertices = sm.vertices;
+    dm.indices = sm.indices;
+    dm.faces = faces;
+    std::vector<uint32_t> start, list;
+    rc = build_face_grid(h->params[scene], vertices, vertex_count, indices, faces, start, list, dm);
+    if (rc >= 256) return rc;
+    if (rc == 0) {
+      if ((rc = dev_alloc(&sm.cell_start, start.size())) || (rc = dev_alloc(&sm.cell_faces, list.size())))
+        return rc;
+      CUDA_TRY(cudaMemcpy(sm.cell_start, start.data(), sizeof(uint32_t) * start.size(), cudaMemcpyHostToDevice));
+      CUDA_TRY(cudaMemcpy(sm.cell_faces, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice));
+      dm.cell_start = sm.cell_start;
+      dm.cell_faces = sm.cell_faces;
+    }
   }
-  return CLSPH_OK;
+  return sync_scene_tables(h);
+}
+
+int clsph_gpu_set_mesh(clsph_gpu* h, const float* normals, const float* vertices,
+                       uint32_t vertex_count, const uint32_t* indices, uint32_t faces) {
+  return clsph_gpu_set_scene_mesh(h, 0, normals, vertices, vertex_count, indices, faces);
 }
 
 int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles) {
   if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "upload: bad argument");
   CUDA_TRY(cudaMemcpyAsync(h->aos_stage, particles, sizeof(clsph_particle) * h->n,
                            cudaMemcpyHostToDevice, h->stream));
-  h->launch(K_MISC, k_bbox_reset, dim3(1), dim3(32), h->bbox);
-  h->launch(K_UNPACK, k_unpack_aos, dim3(grid_blocks(h->n, 152 * 8)), dim3(kBlock),
-            (const float4*)h->aos_stage, h->n, h->st[0], h->bbox, h->status);
+  h->launch(K_MISC, k_bbox_reset, dim3(grid_blocks(6 * h->nscenes, 64)), dim3(kBlock), h->bbox,
+            h->nscenes);
+  h->launch(K_UNPACK, k_unpack_aos, dim3(grid_blocks(h->n, h->sm_count * 8)), dim3(kBlock),
+            (const float4*)h->aos_stage, h->n, h->st[0], (const uint16_t*)h->scene_of, h->bbox,
+            h->status);
   h->uploaded = true;
   h->partial = false;
   h->have_fields = false;
@@ -554,9 +663,9 @@ int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles) {
 int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles) {
   if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "download: bad argument");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "download: no complete state");
-  h->launch(K_PACK, k_pack_aos, dim3(grid_blocks(h->n, 152 * 8)), dim3(kBlock), h->aos_stage, h->n,
-            h->st[0], (const float4*)h->aux, (const uint32_t*)h->keys,
-            (const DevGrid*)h->grid, h->have_fields ? 1 : 0);
+  h->launch(K_PACK, k_pack_aos, dim3(grid_blocks(h->n, h->sm_count * 8)), dim3(kBlock),
+            h->aos_stage, h->n, h->st[0], (const float4*)h->aux, (const uint32_t*)h->keys,
+            (const uint32_t*)h->ctl, h->have_fields ? 1 : 0);
   CUDA_TRY(cudaMemcpyAsync(particles, h->aos_stage, sizeof(clsph_particle) * h->n,
                            cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -566,7 +675,17 @@ int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles) {
 int clsph_gpu_step(clsph_gpu* h, uint32_t substeps) {
   if (!h) return fail(CLSPH_ERR_ARGUMENT, "step: null handle");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step: upload particles first");
-  for (uint32_t s = 0; s < substeps; ++s) {
+  uint32_t done = 0;
+  if (h->use_graph && !h->profiling && substeps >= 2) {
+    int rc = ensure_graph(h);
+    if (rc) return rc;
+    for (; done + 2 <= substeps; done += 2) {
+      CUDA_TRY(cudaGraphLaunch(h->graph_exec[h->ids_sel], h->stream));
+      h->launches += 2 * kLaunchesPerSubstep;
+      h->substeps += 2;
+    }
+  }
+  for (; done < substeps; ++done) {
     int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
     if (rc) return rc;
     ++h->substeps;
@@ -598,12 +717,12 @@ int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags) {
   return CLSPH_OK;
 }
 
-int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out) {
-  if (!h || !out) return fail(CLSPH_ERR_ARGUMENT, "get_parameters: bad argument");
+int clsph_gpu_get_scene_parameters(clsph_gpu* h, uint32_t scene, clsph_parameters* out) {
+  if (!h || !out || scene >= h->nscenes) return fail(CLSPH_ERR_ARGUMENT, "get_parameters: bad argument");
   DevGrid g;
-  int rc = read_grid(h, &g);
+  int rc = read_grid(h, scene, &g, nullptr);
   if (rc) return rc;
-  *out = h->params;
+  *out = h->params[scene];
   for (int a = 0; a < 3; ++a) {
     out->min_point.s[a] = g.lo[a];
     out->max_point.s[a] = g.hi[a];
@@ -616,32 +735,43 @@ int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out) {
   return CLSPH_OK;
 }
 
+int clsph_gpu_get_parameters(clsph_gpu* h, clsph_parameters* out) {
+  return clsph_gpu_get_scene_parameters(h, 0, out);
+}
+
 int clsph_gpu_read_keys(clsph_gpu* h, uint32_t* keys, uint32_t* perm) {
   if (!h || !keys) return fail(CLSPH_ERR_ARGUMENT, "read_keys: bad argument");
-  DevGrid g;
-  int rc = read_grid(h, &g);
+  uint32_t ctl[kCtlWords];
+  int rc = read_grid(h, 0, nullptr, ctl);
   if (rc) return rc;
-  const size_t off = (size_t)sorted_sel(g) * h->n;
+  const size_t off = (size_t)sorted_sel(ctl[kCtlMaxKey]) * h->n;
   CUDA_TRY(cudaMemcpy(keys, h->keys + off, sizeof(uint32_t) * h->n, cudaMemcpyDeviceToHost));
+  const KeySplit split{ctl[kCtlShift]};
+  for (uint32_t i = 0; i < h->n; ++i) keys[i] = split.morton(keys[i]);
   if (perm) CUDA_TRY(cudaMemcpy(perm, h->vals + off, sizeof(uint32_t) * h->n, cudaMemcpyDeviceToHost));
   return CLSPH_OK;
 }
 
-int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap) {
-  if (!h || !table) return fail(CLSPH_ERR_ARGUMENT, "read_cell_table: bad argument");
+int clsph_gpu_read_cell_table_scene(clsph_gpu* h, uint32_t scene, uint32_t* table, uint64_t cap) {
+  if (!h || !table || scene >= h->nscenes) return fail(CLSPH_ERR_ARGUMENT, "read_cell_table: bad argument");
   DevGrid g;
-  int rc = read_grid(h, &g);
+  int rc = read_grid(h, scene, &g, nullptr);
   if (rc) return rc;
   if (cap < g.cells) return fail(CLSPH_ERR_ARGUMENT, "read_cell_table: buffer too small");
   if (g.cells == 0) return CLSPH_OK;
   uint32_t* d = nullptr;
   if ((rc = dev_alloc(&d, g.cells))) return rc;
-  k_dense_table<<<(g.cells + 255) / 256, 256, 0, h->stream>>>(h->keys, h->n, h->grid, d);
+  k_dense_table<<<(g.cells + 255) / 256, 256, 0, h->stream>>>(
+      h->keys, h->n, h->ctl, h->grids + scene, scene, h->scene_first[scene], h->scene_first[scene + 1], d);
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e == cudaSuccess) e = cudaMemcpy(table, d, sizeof(uint32_t) * g.cells, cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("read_cell_table: ") + cudaGetErrorString(e));
   return CLSPH_OK;
+}
+
+int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap) {
+  return clsph_gpu_read_cell_table_scene(h, 0, table, cap);
 }
 
 int clsph_gpu_read_fields(clsph_gpu* h, float* density, float* pressure, float* accel) {

@@ -8,9 +8,14 @@
 //   keys[2][n], vals[2][n]    radix-sort ping-pong (Morton key, source slot)
 //   ids[2][n]                 persistent particle ids (the reference has none)
 //   hkeys[S], hstart[S], hend[S]  cell index: Morton key -> [start, end)
-// The per-substep grid (bounding box, cell size, dense cell count, number
-// of radix passes) lives in device memory (DevGrid) so that no host round
-// trip is needed between kernels.
+// A handle holds S independent scenes (S = 1 for a single simulation): the
+// particles of scene s occupy one contiguous slot range, scene_of[slot] = s.
+// The sort key is (s << scene_shift) | Morton key, so the one stable sort
+// keeps every scene in its range and orders it exactly like a sort of that
+// scene alone. Per-scene grids (bounding box, cell size, dense cell count),
+// constants and meshes live in device arrays; the sort control (largest key,
+// hence the number of radix passes) is shared. Nothing needs a host round
+// trip between kernels.
 #pragma once
 
 #include "clsph_common.cuh"
@@ -34,27 +39,41 @@ enum : uint32_t {
   kFlagNonFinite = 4u,
 };
 
-struct DevGrid {
+struct DevGrid {         // one scene's grid of the current substep
   float lo[3];
   float hi[3];
   float cell;           // 2h
   int32_t size[3];      // grid_size_x/y/z
   uint32_t cells;       // grid_cell_count (dense Morton range)
-  uint32_t maxkey;      // largest key of the substep (sets the radix passes)
   float half_margin;    // rounding margin of the half-cell tests, in cells
-  uint32_t pad_[3];
+  uint32_t pad_[4];
 };
 
 // 8-bit radix passes that cover every key of the substep.
-__host__ __device__ __forceinline__ uint32_t radix_passes(const DevGrid& g) {
-  uint32_t k = g.maxkey | 1u, bits = 0;
+__host__ __device__ __forceinline__ uint32_t radix_passes(uint32_t maxkey) {
+  uint32_t k = maxkey | 1u, bits = 0;
   while (k) { ++bits; k >>= 1; }
   return (bits + 7u) / 8u;
 }
 // Ping-pong buffer that holds the sorted keys and slots after all passes.
-__host__ __device__ __forceinline__ uint32_t sorted_sel(const DevGrid& g) {
-  return radix_passes(g) & 1u;
+__host__ __device__ __forceinline__ uint32_t sorted_sel(uint32_t maxkey) {
+  return radix_passes(maxkey) & 1u;
 }
+
+// Sort control block of a substep (device memory): [0] largest key,
+// [1] Morton bits (widest grid of all scenes), [2] scene bits.
+enum : int { kCtlMaxKey = 0, kCtlShift = 1, kCtlSceneBits = 2, kCtlWords = 8 };
+
+// Scene bits of a sort key and its Morton part.
+struct KeySplit {
+  uint32_t shift;  // Morton keys use bits [0, shift)
+  __host__ __device__ __forceinline__ uint32_t morton(uint32_t key) const {
+    return shift >= 32u ? key : (key & ((1u << shift) - 1u));
+  }
+  __host__ __device__ __forceinline__ uint32_t scene_bits(uint32_t scene) const {
+    return shift >= 32u ? 0u : (scene << shift);
+  }
+};
 
 // Per-substep constants (kernel argument).
 struct Consts {
@@ -159,16 +178,22 @@ __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const
 
 // --------------------------------------------------------------- kernels
 
-// Single-thread grid set-up (sph_simulation.cpp:253-306) from the bounding
-// box accumulated by the previous kernel; resets the box and the radix digit
-// totals for this substep.
-__global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ grid, float h,
+// Grid set-up of every scene (sph_simulation.cpp:253-306), one thread per
+// scene, from the bounding boxes accumulated by the previous kernel; resets
+// the boxes, the radix digit totals and the sort control for this substep.
+__global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
+                             const float* __restrict__ scene_h, uint32_t nscenes,
                              uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
-                             uint32_t* __restrict__ step_counters) {
+                             uint32_t* __restrict__ step_counters, uint32_t* __restrict__ ctl) {
+  __shared__ uint32_t shift_s;
   for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) digit_total[i] = 0u;
   if (threadIdx.x < kStepCounters) step_counters[threadIdx.x] = 0u;
-  if (threadIdx.x != 0) return;
-  const float cell = XMUL(h, 2.f);
+  if (threadIdx.x == 0) shift_s = 1u;
+  __syncthreads();
+  for (uint32_t sc = threadIdx.x; sc < nscenes; sc += blockDim.x) {
+  uint32_t* bbox = bbox_all + 6 * (size_t)sc;
+  DevGrid* grid = grids + sc;
+  const float cell = XMUL(scene_h[sc], 2.f);
   DevGrid g;
   bool overflow = false;
   for (int a = 0; a < 3; ++a) {
@@ -184,13 +209,13 @@ __global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ 
   }
   g.cell = cell;
   g.cells = morton3((uint32_t)g.size[0], (uint32_t)g.size[1], (uint32_t)g.size[2]);
-  g.maxkey = 0u;
+  atomicMax(&shift_s, 32u - __clz(g.cells | 1u));  // keys of this scene are < cells
   // The cell coordinate t = fl(fl(p - lo) / 2h) is within ~2^-22 * t of the
   // exact value and t < grid size G, so 2^-20 * (G + 2) covers its rounding
   // and that of the distance test twice over.
   const int gmax = max(g.size[0], max(g.size[1], g.size[2]));
   g.half_margin = (float)(gmax + 2) * 0x1p-20f;
-  for (int i = 0; i < 3; ++i) g.pad_[i] = 0u;
+  for (int i = 0; i < 4; ++i) g.pad_[i] = 0u;
   *grid = g;
   if (overflow) atomicOr(status, kFlagGridOverflow);
   // sentinels of sph_simulation.cpp:258-259 for the next accumulation
@@ -198,18 +223,49 @@ __global__ void k_grid_setup(uint32_t* __restrict__ bbox, DevGrid* __restrict__ 
     bbox[a] = f2ord(2147483648.0f);
     bbox[3 + a] = f2ord(-2147483648.0f);
   }
-}
-
-__global__ void k_bbox_reset(uint32_t* __restrict__ bbox) {
-  if (threadIdx.x < 3) {
-    bbox[threadIdx.x] = f2ord(2147483648.0f);
-    bbox[3 + threadIdx.x] = f2ord(-2147483648.0f);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl[kCtlMaxKey] = 0u;
+    ctl[kCtlShift] = shift_s;
+    // scene bits above the Morton bits must fit in 32 (batched scenes)
+    if (shift_s + ctl[kCtlSceneBits] > 32u) atomicOr(status, kFlagGridOverflow);
   }
 }
 
-// Block-level min/max of positions, then one atomic per block and axis.
-// NaN coordinates are ignored, as the reference's `<` / `>` tests do.
-__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, uint32_t* bbox) {
+__global__ void k_bbox_reset(uint32_t* __restrict__ bbox, uint32_t nscenes) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < 6 * nscenes; k += gridDim.x * blockDim.x)
+    bbox[k] = (k % 6) < 3 ? f2ord(2147483648.0f) : f2ord(-2147483648.0f);
+}
+
+// Per-scene min/max of positions: a block whose threads all saw one scene
+// reduces to one atomic per axis; otherwise every warp (or, across a scene
+// boundary, every thread) adds its own. NaN coordinates are ignored, as the
+// reference's `<` / `>` tests do. A thread with no particle passes scene = -1.
+__device__ __forceinline__ void bbox_atomics(const float v[6], uint32_t* bbox) {
+  if (v[0] == v[0]) atomicMin(&bbox[0], f2ord(v[0]));
+  if (v[1] == v[1]) atomicMin(&bbox[1], f2ord(v[1]));
+  if (v[2] == v[2]) atomicMin(&bbox[2], f2ord(v[2]));
+  if (v[3] == v[3]) atomicMax(&bbox[3], f2ord(v[3]));
+  if (v[4] == v[4]) atomicMax(&bbox[4], f2ord(v[4]));
+  if (v[5] == v[5]) atomicMax(&bbox[5], f2ord(v[5]));
+}
+
+__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene, uint32_t* bbox_all) {
+  __shared__ int block_scene;
+  if (threadIdx.x == 0) block_scene = -2;
+  __syncthreads();
+  if (scene >= 0) atomicCAS(&block_scene, -2, scene);
+  __syncthreads();
+  const int s0 = block_scene;
+  const bool uniform = __syncthreads_and(scene < 0 || scene == s0);
+  if (!uniform) {
+    const float v[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+    if (scene >= 0) bbox_atomics(v, bbox_all + 6 * (size_t)scene);
+    return;
+  }
+  if (s0 < 0) return;
+  uint32_t* bbox = bbox_all + 6 * (size_t)s0;
   __shared__ float red[6][kBlock / 32];
   float v[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
 #pragma unroll
@@ -246,30 +302,38 @@ __device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, uint32_t* 
 
 // Host AoS (80-byte particle) -> SoA state, with bounding box.
 __global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State st,
-                             uint32_t* __restrict__ bbox, uint32_t* __restrict__ status) {
+                             const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ bbox,
+                             uint32_t* __restrict__ status) {
   const float qnan = __int_as_float(0x7FC00000);
-  float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
+    int scene = -1;
+    if (i < n) {
     const float4* p = aos + (size_t)i * 5;
-    float4 pos = p[0], vel = p[1], ivel = p[2];
+      float4 pos = p[0], vel = p[1], ivel = p[2];
     pos.w = 0.f;
     vel.w = 0.f;
     ivel.w = 0.f;
     st.pos[i] = pos;
     st.vel[i] = vel;
     st.ivel[i] = ivel;
-    lo = make_float3(fminf(lo.x, pos.x), fminf(lo.y, pos.y), fminf(lo.z, pos.z));
-    hi = make_float3(fmaxf(hi.x, pos.x), fmaxf(hi.y, pos.y), fmaxf(hi.z, pos.z));
+    lo = make_float3(pos.x, pos.y, pos.z);
+    hi = lo;
+    scene = scene_of[i];
     if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
+    }
+    bbox_accumulate(lo, hi, scene, bbox);
   }
-  bbox_accumulate(lo, hi, bbox);
 }
 
 // SoA -> host AoS: acceleration is 0 after the advection loop (sph.cl:97-99).
 __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
                            const float4* __restrict__ aux, const uint32_t* __restrict__ keys_base,
-                           const DevGrid* __restrict__ grid, int have_fields) {
-  const uint32_t sel = have_fields ? sorted_sel(*grid) : 0u;
+                           const uint32_t* __restrict__ ctl, int have_fields) {
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t sel = have_fields ? sorted_sel(ctl[kCtlMaxKey]) : 0u;
   const uint32_t* keys = keys_base + (size_t)sel * n;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4* p = aos + (size_t)i * 5;
@@ -281,7 +345,7 @@ __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
     const float4 a = have_fields ? aux[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     tail.x = a.x;
     tail.y = a.y;
-    tail.z = __uint_as_float(have_fields ? keys[i] : 0u);
+    tail.z = __uint_as_float(have_fields ? split.morton(keys[i]) : 0u);
     tail.w = 0.f;
     p[4] = tail;
   }
@@ -289,26 +353,29 @@ __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
 
 // Morton key per particle (grid.cl:56-66) and the largest key.
 __global__ void __launch_bounds__(kBlock)
-    k_keys(const float4* __restrict__ pos, uint32_t n, DevGrid* __restrict__ grid,
+    k_keys(const float4* __restrict__ pos, uint32_t n, const DevGrid* __restrict__ grids,
+           const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
            uint32_t* __restrict__ keys) {
+  const KeySplit split{ctl[kCtlShift]};
   __shared__ uint32_t block_max;
   if (threadIdx.x == 0) block_max = 0u;
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t key = 0u;
   if (i < n) {
-    const DevGrid& g = *grid;
+    const uint32_t sc = scene_of[i];
+    const DevGrid& g = grids[sc];
     const float4 p = pos[i];
     uint32_t cx = __float2uint_rz(XDIV(XSUB(p.x, g.lo[0]), g.cell));
     uint32_t cy = __float2uint_rz(XDIV(XSUB(p.y, g.lo[1]), g.cell));
     uint32_t cz = __float2uint_rz(XDIV(XSUB(p.z, g.lo[2]), g.cell));
-    key = morton3(cx, cy, cz);
+    key = morton3(cx, cy, cz) | split.scene_bits(sc);
     keys[i] = key;
   }
   key = __reduce_max_sync(0xFFFFFFFFu, key);
   if ((threadIdx.x & 31) == 0) atomicMax(&block_max, key);
   __syncthreads();
-  if (threadIdx.x == 0) atomicMax(&grid->maxkey, block_max);
+  if (threadIdx.x == 0) atomicMax(&ctl[kCtlMaxKey], block_max);
 }
 
 // ---------------------------------------------------------------- radix sort
@@ -317,9 +384,9 @@ __global__ void __launch_bounds__(kBlock)
 // launch sequence is fixed (graph-capturable) while the work follows the
 // key width. Ping-pong: pass p reads buffer p&1 and writes (p+1)&1.
 __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
-                              const DevGrid* __restrict__ grid, uint32_t* __restrict__ tile_hist,
+                              const uint32_t* __restrict__ ctl, uint32_t* __restrict__ tile_hist,
                               uint32_t ntiles, uint32_t* __restrict__ digit_total) {
-  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t hist[256];
   hist[threadIdx.x] = 0u;
   __syncthreads();
@@ -340,9 +407,9 @@ __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n
 // One block per digit: exclusive scan of that digit's per-tile counts plus
 // the number of keys with a smaller digit.
 __global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, int pass,
-                             const DevGrid* __restrict__ grid,
+                             const uint32_t* __restrict__ ctl,
                              const uint32_t* __restrict__ digit_total) {
-  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t warp_sums[kRadixThreads / 32];
   __shared__ uint32_t base_s;
   const uint32_t d = blockIdx.x;
@@ -384,9 +451,9 @@ __global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, 
 
 __global__ void __launch_bounds__(kRadixThreads)
     k_radix_scatter(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
-                    int pass, const DevGrid* __restrict__ grid,
+                    int pass, const uint32_t* __restrict__ ctl,
                     const uint32_t* __restrict__ tile_hist, uint32_t ntiles) {
-  if ((uint32_t)pass >= radix_passes(*grid)) return;
+  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t cnt[kRadixWarps][256];
   __shared__ uint32_t tile_off[256];
   const uint32_t* keys_in = keys_base + (size_t)(pass & 1) * n;
@@ -439,7 +506,8 @@ __global__ void __launch_bounds__(kRadixThreads)
 // Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
 // and records every cell's [start, end) in the cell index (the dense cell
 // table of sph_simulation.cpp:216-224 in compact form).
-__global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grid,
+__global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
+                         const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
                          const uint32_t* __restrict__ keys_base,
                          const uint32_t* __restrict__ vals_base, State src, State dst,
                          const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
@@ -447,13 +515,14 @@ __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grid,
                          uint32_t* __restrict__ cell_count) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const uint32_t sel = sorted_sel(*grid);
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t sel = sorted_sel(ctl[kCtlMaxKey]);
   const uint32_t* keys = keys_base + (size_t)sel * n;
   const uint32_t* perm = vals_base + (size_t)sel * n;
   const uint32_t from = perm[s];
   const uint32_t key = keys[s];
   float4 p = src.pos[from];
-  p.w = __uint_as_float(half_code(p, key, *grid));
+  p.w = __uint_as_float(half_code(p, split.morton(key), grids[scene_of[s]]));
   dst.pos[s] = p;
   dst.vel[s] = src.vel[from];
   dst.ivel[s] = src.ivel[from];
@@ -563,11 +632,12 @@ __device__ __forceinline__ float4 finish_accel(const ForceSums& f, float rho_i, 
 
 // Calls f(j) for every candidate of particle i's window in the reference's order.
 template <class F>
-__device__ __forceinline__ void for_each_candidate(const Window& w, const CellIndex& ci, F&& f) {
+__device__ __forceinline__ void for_each_candidate(const Window& w, uint32_t sbits,
+                                                   const CellIndex& ci, F&& f) {
   for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
     for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
       for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
-        const uint2 r = cell_lookup(ci, morton3(x, y, z));
+        const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
         for (uint32_t j = r.x; j < r.y; ++j) f(j);
       }
 }
@@ -599,14 +669,14 @@ __device__ __forceinline__ uint32_t facing_mask(int ox, int oy, int oz) {
 
 template <class F>
 __device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint32_t key,
-                                                          const CellIndex& ci,
+                                                          uint32_t sbits, const CellIndex& ci,
                                                           const float4* __restrict__ pos, F&& f) {
   const int c[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
   for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
     for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
       for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
         const uint32_t need = facing_mask((int)x - c[0], (int)y - c[1], (int)z - c[2]);
-        const uint2 r = cell_lookup(ci, morton3(x, y, z));
+        const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
         for (uint32_t j = r.x; j < r.y; ++j) {
           const float4 pj = __ldg(&pos[j]);
           if ((__float_as_uint(pj.w) & need) == need) f(j, pj);
@@ -615,20 +685,25 @@ __device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint3
 }
 
 __global__ void __launch_bounds__(kGatherBlock)
-    k_density(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
-              const float4* __restrict__ pos, CellIndex ci, Consts c, float4* __restrict__ aux_out,
+    k_density(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+              const uint32_t* __restrict__ ctl,
+              const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos, CellIndex ci,
+              const Consts* __restrict__ consts, float4* __restrict__ aux_out,
               uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap) {
   __shared__ uint32_t cand[kScanCap][kGatherBlock];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const DevGrid g = *grid;
-  const uint32_t* keys = keys_base + (size_t)sorted_sel(g) * n;
-  const uint32_t key = keys[i];
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t sc = scene_of[i];
+  const Consts c = consts[sc];
+  const uint32_t sbits = split.scene_bits(sc);
+  const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
+  const uint32_t key = split.morton(keys[i]);
   const float4 pi = pos[i];
-  const Window w = neighbour_window(pi, key, g);
+  const Window w = neighbour_window(pi, key, grids[sc]);
   const float hh = XMUL(c.h, c.h);
   uint32_t found = 0;
-  for_each_facing_candidate(w, key, ci, pos, [&](uint32_t j, float4 pj) {
+  for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) {
       if (found < kScanCap) cand[found][threadIdx.x] = j;
@@ -652,7 +727,7 @@ __global__ void __launch_bounds__(kGatherBlock)
       visit(j, __ldg(&pos[j]));
     }
   } else {
-    for_each_facing_candidate(w, key, ci, pos, [&](uint32_t j, float4 pj) {
+    for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
       const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj);
     });
@@ -664,12 +739,16 @@ __global__ void __launch_bounds__(kGatherBlock)
 // Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58), walking
 // the neighbour list of k_density (or the window, for overflowing lists).
 __global__ void __launch_bounds__(kGatherBlock)
-    k_forces(uint32_t n, const DevGrid* __restrict__ grid, const uint32_t* __restrict__ keys_base,
-             State st, const float4* __restrict__ aux, CellIndex ci, Consts c,
-             const uint32_t* __restrict__ nlist, const uint32_t* __restrict__ ncount,
-             uint32_t nlist_cap, float4* __restrict__ acc_out) {
+    k_forces(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+             const uint32_t* __restrict__ ctl,
+             const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,
+             CellIndex ci, const Consts* __restrict__ consts, const uint32_t* __restrict__ nlist,
+             const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
+             float4* __restrict__ acc_out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const uint32_t sc = scene_of[i];
+  const Consts c = consts[sc];
   const float4 pi = st.pos[i];
   const float4 vi = st.vel[i];
   const float4 ai = aux[i];
@@ -687,10 +766,10 @@ __global__ void __launch_bounds__(kGatherBlock)
   if (cnt <= nlist_cap) {
     for (uint32_t k = 0; k < cnt; ++k) pair(__ldg(&nlist[(size_t)k * n + i]));
   } else {
-    const DevGrid g = *grid;
-    const uint32_t* keys = keys_base + (size_t)sorted_sel(g) * n;
-    const Window w = neighbour_window(pi, keys[i], g);
-    for_each_candidate(w, ci, [&](uint32_t j) {
+    const KeySplit split{ctl[kCtlShift]};
+    const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
+    const Window w = neighbour_window(pi, split.morton(keys[i]), grids[sc]);
+    for_each_candidate(w, split.scene_bits(sc), ci, [&](uint32_t j) {
       const float4 pj = __ldg(&st.pos[j]);
       const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > c.cull_r2) return;
@@ -776,12 +855,20 @@ __device__ __forceinline__ bool nearest_hit(const DevMesh& m, V3 p0, V3 p1, Hit&
 // collisions.cl:91-129), capped at max_iters passes; writes the new state
 // into `out` (same slots) and accumulates the next bounding box.
 __global__ void __launch_bounds__(kBlock)
-    k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out, DevMesh m, Consts c,
-             uint32_t max_iters, uint32_t* __restrict__ bbox, uint32_t* __restrict__ status,
-             unsigned long long* __restrict__ capped_count) {
+    k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out,
+             const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
+             const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
+             uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count) {
   const float qnan = __int_as_float(0x7FC00000);
-  float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
+    int scene = -1;
+    if (i < n) {
+    scene = scene_of[i];
+    const Consts& c = consts[scene];
+    const DevMesh m = meshes[scene];
     float remaining = XMUL(c.time_delta, c.scale);
     V3 pos = v3(in.pos[i]);
     const V3 vh_old = v3(in.ivel[i]);
@@ -828,25 +915,31 @@ __global__ void __launch_bounds__(kBlock)
     out.vel[i] = make_float4(XDIV(XADD(vh_old.x, v.x), 2.f), XDIV(XADD(vh_old.y, v.y), 2.f),
                              XDIV(XADD(vh_old.z, v.z), 2.f), 0.f);
     if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
-    lo = make_float3(fminf(lo.x, pos.x), fminf(lo.y, pos.y), fminf(lo.z, pos.z));
-    hi = make_float3(fmaxf(hi.x, pos.x), fmaxf(hi.y, pos.y), fmaxf(hi.z, pos.z));
+    lo = make_float3(pos.x, pos.y, pos.z);
+    hi = lo;
+    }
+    bbox_accumulate(lo, hi, scene, bbox);
   }
-  bbox_accumulate(lo, hi, bbox);
 }
 
-// Dense reference cell table from the sorted keys: table[c] = lower_bound(c).
+// Dense reference cell table of one scene from the sorted keys of its slot
+// range [first, last): table[c] = lower_bound(c) - first, c < cells.
 __global__ void k_dense_table(const uint32_t* __restrict__ keys_base, uint32_t n,
-                              const DevGrid* __restrict__ grid, uint32_t* __restrict__ table) {
+                              const uint32_t* __restrict__ ctl, const DevGrid* __restrict__ grid,
+                              uint32_t scene, uint32_t first, uint32_t last,
+                              uint32_t* __restrict__ table) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t cells = grid->cells;
   if (c >= cells) return;
-  const uint32_t* keys = keys_base + (size_t)(sorted_sel(*grid)) * n;
-  uint32_t lo = 0, hi = n;
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
+  const uint32_t want = c | split.scene_bits(scene);
+  uint32_t lo = first, hi = last;
   while (lo < hi) {
     uint32_t mid = lo + (hi - lo) / 2;
-    if (keys[mid] < c) lo = mid + 1; else hi = mid;
+    if (keys[mid] < want) lo = mid + 1; else hi = mid;
   }
-  table[c] = lo;
+  table[c] = lo - first;
 }
 
 }  // namespace clsph

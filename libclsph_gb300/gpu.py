@@ -26,6 +26,11 @@ _u32 = ctypes.c_uint32
 # (name, restype, argtypes) of every symbol include/clsph_gpu.h declares
 SIGNATURES = [
     ("clsph_gpu_create", ctypes.c_int, [_vp, _vp, _u32, ctypes.POINTER(_vp)]),
+    ("clsph_gpu_create_batched", ctypes.c_int, [_vp, _vp, _vp, _u32, ctypes.POINTER(_vp)]),
+    ("clsph_gpu_set_scene_mesh", ctypes.c_int, [_vp, _u32, _vp, _vp, _u32, _vp, _u32]),
+    ("clsph_gpu_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("clsph_gpu_get_scene_parameters", ctypes.c_int, [_vp, _u32, _vp]),
+    ("clsph_gpu_read_cell_table_scene", ctypes.c_int, [_vp, _u32, _vp, ctypes.c_uint64]),
     ("clsph_gpu_destroy", ctypes.c_int, [_vp]),
     ("clsph_gpu_set_collision_cap", ctypes.c_int, [_vp, _u32]),
     ("clsph_gpu_set_stream", ctypes.c_int, [_vp, _vp]),
@@ -94,21 +99,45 @@ def _a(x: np.ndarray) -> int:
 
 
 class GpuSolver:
-    """One SPH scene on the current CUDA device (include/clsph_gpu.h)."""
+    """SPH scenes on the current CUDA device (include/clsph_gpu.h).
 
-    def __init__(self, params, terms, n: int | None = None, mesh=None):
+    `GpuSolver(params, terms, n, mesh)` holds one scene;
+    `GpuSolver.batched(params_list, terms_list, counts, meshes)` holds several
+    independent scenes stepped by the same kernel launches (their particles
+    are concatenated in scene order in upload/download)."""
+
+    def __init__(self, params, terms, n: int | None = None, mesh=None, *, counts=None):
         self.lib = load_library()
-        self.params = np.array(params, dtype=PARAMS).reshape(1).copy()
-        self.terms = np.array(terms, dtype=TERMS).reshape(1).copy()
-        self.n = int(n if n is not None else self.params["particles_count"][0])
-        self.params["particles_count"] = self.n
+        self.params = np.array(params, dtype=PARAMS).reshape(-1).copy()
+        self.terms = np.array(terms, dtype=TERMS).reshape(-1).copy()
         handle = _vp()
-        _check("clsph_gpu_create",
-               self.lib.clsph_gpu_create(_a(self.params), _a(self.terms), self.n,
-                                         ctypes.byref(handle)))
+        if counts is None:
+            self.counts = [int(n if n is not None else self.params["particles_count"][0])]
+            self.params["particles_count"] = self.counts[0]
+            _check("clsph_gpu_create",
+                   self.lib.clsph_gpu_create(_a(self.params), _a(self.terms), self.counts[0],
+                                             ctypes.byref(handle)))
+        else:
+            self.counts = [int(c) for c in counts]
+            cnt = np.array(self.counts, dtype=np.uint32)
+            self.params["particles_count"] = cnt
+            _check("clsph_gpu_create_batched",
+                   self.lib.clsph_gpu_create_batched(_a(self.params), _a(self.terms), _a(cnt),
+                                                     len(cnt), ctypes.byref(handle)))
+        self.n = int(sum(self.counts))
+        self.first = np.concatenate([[0], np.cumsum(self.counts)]).astype(np.int64)
         self.h = handle
         if mesh is not None:
             self.set_mesh(mesh)
+
+    @classmethod
+    def batched(cls, params_list, terms_list, counts, meshes=None):
+        g = cls(np.array(list(params_list), dtype=PARAMS), np.array(list(terms_list), dtype=TERMS),
+                counts=counts)
+        for s, m in enumerate(meshes or []):
+            if m is not None:
+                g.set_mesh(m, scene=s)
+        return g
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -134,17 +163,21 @@ class GpuSolver:
     def set_collision_cap(self, iterations: int) -> None:
         _check("clsph_gpu_set_collision_cap", self.lib.clsph_gpu_set_collision_cap(self.h, iterations))
 
-    def set_mesh(self, mesh) -> None:
+    def set_mesh(self, mesh, scene: int = 0) -> None:
         normals = np.ascontiguousarray(mesh["face_normals"], dtype=np.float32)
         verts = np.ascontiguousarray(mesh["vertices"], dtype=np.float32)
         idx = np.ascontiguousarray(mesh["indices"], dtype=np.uint32)
         faces = len(idx) // 3
         if faces == 0:
-            _check("clsph_gpu_set_mesh", self.lib.clsph_gpu_set_mesh(self.h, None, None, 0, None, 0))
+            _check("clsph_gpu_set_scene_mesh",
+                   self.lib.clsph_gpu_set_scene_mesh(self.h, scene, None, None, 0, None, 0))
             return
-        _check("clsph_gpu_set_mesh",
-               self.lib.clsph_gpu_set_mesh(self.h, _a(normals), _a(verts), len(verts) // 3, _a(idx),
-                                           faces))
+        _check("clsph_gpu_set_scene_mesh",
+               self.lib.clsph_gpu_set_scene_mesh(self.h, scene, _a(normals), _a(verts),
+                                                 len(verts) // 3, _a(idx), faces))
+
+    def set_graph(self, on: bool) -> None:
+        _check("clsph_gpu_set_graph", self.lib.clsph_gpu_set_graph(self.h, 1 if on else 0))
 
     # ------------------------------------------------------------ transfers
     def upload(self, particles: np.ndarray) -> None:
@@ -173,9 +206,10 @@ class GpuSolver:
         return flags.value
 
     # ------------------------------------------------------------ inspection
-    def parameters(self) -> np.void:
+    def parameters(self, scene: int = 0) -> np.void:
         out = np.zeros(1, dtype=PARAMS)
-        _check("clsph_gpu_get_parameters", self.lib.clsph_gpu_get_parameters(self.h, _a(out)))
+        _check("clsph_gpu_get_scene_parameters",
+               self.lib.clsph_gpu_get_scene_parameters(self.h, scene, _a(out)))
         return out[0]
 
     def keys(self):
@@ -184,11 +218,11 @@ class GpuSolver:
         _check("clsph_gpu_read_keys", self.lib.clsph_gpu_read_keys(self.h, _a(keys), _a(perm)))
         return keys, perm
 
-    def cell_table(self) -> np.ndarray:
-        cells = int(self.parameters()["grid_cell_count"])
+    def cell_table(self, scene: int = 0) -> np.ndarray:
+        cells = int(self.parameters(scene)["grid_cell_count"])
         table = np.zeros(max(cells, 1), dtype=np.uint32)
-        _check("clsph_gpu_read_cell_table",
-               self.lib.clsph_gpu_read_cell_table(self.h, _a(table), cells))
+        _check("clsph_gpu_read_cell_table_scene",
+               self.lib.clsph_gpu_read_cell_table_scene(self.h, scene, _a(table), cells))
         return table[:cells]
 
     def fields(self):
