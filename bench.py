@@ -56,11 +56,48 @@ ALG_BYTES_PER_PARTICLE = {
 }
 STEP_ALG_BYTES = 232  # per particle-substep: key read 16 + sort scatter 96 + density 20 + forces/integrate 100
 
+def _w():
+    return __import__("libclsph_gb300.workloads", fromlist=["x"])
+
+
 WORKLOADS = {
-    "dam_break_1m": lambda: __import__("libclsph_gb300.workloads", fromlist=["x"]).dam_break_1m(),
-    "dam_break_32k": lambda: __import__("libclsph_gb300.workloads", fromlist=["x"]).dam_break_32k(),
-    "pour_4m": lambda: __import__("libclsph_gb300.workloads", fromlist=["x"]).pour(),
+    "dam_break_1m": lambda: _w().dam_break_1m(),
+    "dam_break_32k": lambda: _w().dam_break_32k(),
+    "pour_4m": lambda: _w().pour(),
+    "batched_256": lambda: _w().batched_dam_breaks(256),
 }
+
+
+class Batch:
+    """A list of scenes run by one batched handle."""
+
+    def __init__(self, scenes):
+        self.scenes = scenes
+        self.name = f"batched_{len(scenes)}_dam_breaks"
+        self.particles = np.concatenate([s.particles for s in scenes])
+        self.params = scenes[0].params
+        self.mesh = scenes[0].mesh
+        self.info = {"scenes": len(scenes), "n_min": min(s.n for s in scenes),
+                     "n_max": max(s.n for s in scenes)}
+
+    @property
+    def n(self):
+        return len(self.particles)
+
+
+def load_workload(name):
+    w = WORKLOADS[name]()
+    return Batch(w) if isinstance(w, list) else w
+
+
+def make_solver(scene):
+    from libclsph_gb300.gpu import GpuSolver
+
+    if isinstance(scene, Batch):
+        sc = scene.scenes
+        return GpuSolver.batched([s.params for s in sc], [s.terms for s in sc], [s.n for s in sc],
+                                 [s.mesh for s in sc])
+    return GpuSolver(scene.params, scene.terms, scene.n, scene.mesh)
 
 
 def log(*a):
@@ -191,6 +228,19 @@ def cpu_baseline(scene, target_s: float = 12.0) -> dict:
 
     o = Oracle()
     threads = os.cpu_count() or 1
+    if isinstance(scene, Batch):  # scenes one after another, as many as the budget allows
+        done = 0
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < target_s and k < len(scene.scenes):
+            sc = scene.scenes[k]
+            o.run(sc.params, sc.terms, sc.particles, 1, sc.mesh, threads=threads)
+            done += sc.n
+            k += 1
+        dt = time.perf_counter() - t0
+        return {"value": done / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                "sample": f"one substep of each of the first {k} of {len(scene.scenes)} scenes "
+                          f"({done} particle-steps, {dt:.1f} s, OpenMP over particles)"}
     n = scene.n
     steps = 0
     t0 = time.perf_counter()
@@ -211,17 +261,33 @@ def run_reference(args, world, rank) -> None:
         return
     from oracle import Oracle
 
-    scene = WORKLOADS[args.workload]()
-    sample_n = min(65536, scene.n)
-    sample = cpu_sample_scene(scene, sample_n)
+    scene = load_workload(args.workload)
+    if isinstance(scene, Batch):  # the first scenes, up to ~65k particles
+        take, tot = [], 0
+        for sc in scene.scenes:
+            if tot >= 65536:
+                break
+            take.append(sc)
+            tot += sc.n
+        sample_n = tot
+        sample = None
+    else:
+        sample_n = min(65536, scene.n)
+        sample = cpu_sample_scene(scene, sample_n)
     o = Oracle()
     threads = os.cpu_count() or 1
-    cur = sample.particles
+    units = [sample] if sample is not None else take
+    cur = [u.particles for u in units]
+
+    def one_step():
+        for k, u in enumerate(units):
+            cur[k] = o.run(u.params, u.terms, cur[k], 1, u.mesh, threads=threads)
+
     for _ in range(args.warmup):
-        cur = o.run(sample.params, sample.terms, cur, 1, sample.mesh, threads=threads)
+        one_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cur = o.run(sample.params, sample.terms, cur, 1, sample.mesh, threads=threads)
+        one_step()
     dt = time.perf_counter() - t0
     value = sample_n * args.steps / dt
     line = {
@@ -251,6 +317,8 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="launch every kernel instead of replaying a CUDA graph")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -266,34 +334,41 @@ def main() -> None:
 
     torch.cuda.set_device(local)
     load_library()
-    scene = WORKLOADS[args.workload]()
+    scene = load_workload(args.workload)
     n = scene.n
-    log(f"[rank {rank}] {scene.name}: n={n}, faces={len(scene.mesh['indices']) // 3}")
+    log(f"[rank {rank}] {scene.name}: n={n}")
     stream = torch.cuda.Stream()
-    solver = GpuSolver(scene.params, scene.terms, n, scene.mesh)
+    solver = make_solver(scene)
     solver.set_stream(stream.cuda_stream)
     solver.upload(scene.particles)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tuning = None
+    if not args.no_autotune:
+        tuning = solver.autotune(3)
+        log(tuning)
+    unit = 1 if args.no_graph else 2  # substeps per timed launch unit
+    solver.set_graph(not args.no_graph)
+    args.steps = max(unit, args.steps - args.steps % unit)
 
-    for _ in range(args.warmup):
-        solver.step(1)
+    for _ in range(max(1, args.warmup // unit)):
+        solver.step(unit)
     flags = solver.sync()
 
     # ---- timed region: K substeps on resident particles
     solver.set_profiling(True)
     launches0 = solver.counters()["launches"]
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
+          for _ in range(args.steps // unit)]
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
-            for k in range(args.steps):
+            for k in range(args.steps // unit):
                 if not args.no_flush:
                     flush.fill_(float(k))
                 ev[k][0].record(stream)
-                solver.step(1)
+                solver.step(unit)
                 ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
@@ -301,6 +376,15 @@ def main() -> None:
     step_ms = [a.elapsed_time(b) for a, b in ev]
     flags |= solver.sync()
     launches = solver.counters()["launches"] - launches0
+    solver.set_profiling(False)
+    # per-kernel durations: a separate pass with events around every kernel
+    # (graph replay has no per-kernel events), same state, no flush
+    solver.set_profiling(True)
+    with torch.cuda.stream(stream):
+        for _ in range(min(args.steps, 40)):
+            solver.step(1)
+    torch.cuda.synchronize()
+    prof_steps = min(args.steps, 40)
     ktimes = solver.kernel_times()
     solver.set_profiling(False)
     device_s = sum(step_ms) / 1e3
@@ -308,7 +392,7 @@ def main() -> None:
     total_particles = sum_over_ranks(float(n), world)
     value = total_particles * args.steps / device_s_max
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers (one substep per transfer pair)
     host = torch.empty(n * PARTICLE.itemsize, dtype=torch.uint8, pin_memory=True)
     aos = host.numpy().view(PARTICLE)
     aos[:] = solver.download()
@@ -367,6 +451,7 @@ def main() -> None:
             "lattice": scene.info.get("lattice"),
             "box_m": scene.info.get("box"),
             "h_m": scene.info.get("h"),
+            "scenes": scene.info.get("scenes", 1),
             "faces": len(scene.mesh["indices"]) // 3,
             "l2": "256 MiB buffer written before every timed step, outside the step's events"
                   if not args.no_flush else "no flush",
@@ -387,7 +472,8 @@ def main() -> None:
             "step_alg_GBps": step_achieved,
             "step_frac": step_achieved / peak,
         },
-        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items() if v[1]},
+        "kernel_ms_per_step": {k: v[0] / prof_steps for k, v in ktimes.items() if v[1]},
+        "launch": {"graph": not args.no_graph, "autotune": tuning.strip().splitlines()[-1] if tuning else None},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": n * PARTICLE.itemsize,

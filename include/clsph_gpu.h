@@ -181,6 +181,19 @@ int clsph_gpu_set_profiling(clsph_gpu* h, int enabled);
 int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_stride,
                            float* ms, uint32_t* counts, int* n_classes);
 
+/* Autotuner (no counterpart in the reference): times the density and forces
+ * kernels at 64/128/256 threads per block and the advection grid at 4/8/16
+ * blocks per SM, `substeps` substeps per trial, on the handle's current
+ * particles, keeps the fastest shapes and restores the particle state (the
+ * trials leave the simulation where it was). `report` (may be NULL) receives
+ * the timings as text. Requires an uploaded state. */
+int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report_len);
+
+/* Sets the launch shapes directly (e.g. from a cached autotune result):
+ * blocks of 64, 128 or 256 threads; 1..64 advection blocks per SM. */
+int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block,
+                               uint32_t advect_blocks_per_sm);
+
 /* Counters since create: [0] substeps, [1] particles whose collision loop hit
  * the cap, [2] kernel launches. */
 int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3);

@@ -157,6 +157,11 @@ struct clsph_gpu {
   unsigned long long* capped = nullptr;
   float4* aos_stage = nullptr;
 
+  // launch shapes chosen by clsph_gpu_autotune
+  int density_block = 128;
+  int forces_block = 128;
+  uint32_t advect_blocks_per_sm = 8;
+
   bool uploaded = false;
   bool partial = false;
   bool have_fields = false;
@@ -279,18 +284,36 @@ int enqueue_substep(clsph_gpu* h, int until) {
             h->ids[dst_ids], h->ci, h->cell_list, h->step_counters + kCntCells);
   h->ids_sel = dst_ids;
   if (until <= CLSPH_STAGE_SORT) return 0;
-  const uint32_t gblocks = (n + kGatherBlock - 1) / kGatherBlock;
-  h->launch(K_DENSITY, k_density, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grids,
-            (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
-            (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
-            h->ncount, h->nlist_cap);
+  {
+    const int b = h->density_block;
+    const dim3 grid((n + b - 1) / b);
+    auto args = [&](auto kernel) {
+      h->launch(K_DENSITY, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
+                (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
+                (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
+                h->ncount, h->nlist_cap);
+    };
+    if (b == 64) args(k_density<64>);
+    else if (b == 256) args(k_density<256>);
+    else args(k_density<128>);
+  }
   if (until <= CLSPH_STAGE_DENSITY) return 0;
-  h->launch(K_FORCES, k_forces, dim3(gblocks), dim3(kGatherBlock), n, (const DevGrid*)h->grids,
-            (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
-            (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-            (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
+  {
+    const int b = h->forces_block;
+    const dim3 grid((n + b - 1) / b);
+    auto args = [&](auto kernel) {
+      h->launch(K_FORCES, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
+                (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
+                (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
+                (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
+    };
+    if (b == 64) args(k_forces<64>);
+    else if (b == 256) args(k_forces<256>);
+    else args(k_forces<128>);
+  }
   if (until <= CLSPH_STAGE_FORCES) return 0;
-  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, h->sm_count * 8)), dim3(kBlock), n, h->st[1],
+  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
+            dim3(kBlock), n, h->st[1],
             (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes, (const Consts*)h->consts,
             (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status, h->capped);
   return 0;
@@ -820,6 +843,115 @@ int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_
     if (counts) counts[k] = h->class_count[k];
   }
   if (n_classes) *n_classes = K_NUM_CLASSES;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report_len) {
+  if (!h || substeps == 0) return fail(CLSPH_ERR_ARGUMENT, "autotune: bad argument");
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "autotune: upload particles first");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  // snapshot of the state the trials advance, restored afterwards
+  const size_t n = h->n;
+  float4* snap = nullptr;
+  uint32_t* snap_ids = nullptr;
+  uint32_t* snap_bbox = nullptr;
+  int rc;
+  if ((rc = dev_alloc(&snap, 3 * n)) || (rc = dev_alloc(&snap_ids, n)) ||
+      (rc = dev_alloc(&snap_bbox, 6 * (size_t)h->nscenes))) {
+    cudaFree(snap);
+    cudaFree(snap_ids);
+    return rc;
+  }
+  auto save = [&](bool back) {
+    float4* dst[3] = {h->st[0].pos, h->st[0].vel, h->st[0].ivel};
+    for (int k = 0; k < 3; ++k) {
+      if (back)
+        cudaMemcpyAsync(dst[k], snap + k * n, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream);
+      else
+        cudaMemcpyAsync(snap + k * n, dst[k], sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream);
+    }
+    if (back) {
+      cudaMemcpyAsync(h->ids[h->ids_sel], snap_ids, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, h->stream);
+      cudaMemcpyAsync(h->bbox, snap_bbox, sizeof(uint32_t) * 6 * h->nscenes, cudaMemcpyDeviceToDevice, h->stream);
+    } else {
+      cudaMemcpyAsync(snap_ids, h->ids[h->ids_sel], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, h->stream);
+      cudaMemcpyAsync(snap_bbox, h->bbox, sizeof(uint32_t) * 6 * h->nscenes, cudaMemcpyDeviceToDevice, h->stream);
+    }
+  };
+  save(false);
+  const int ids_sel0 = h->ids_sel;
+  const bool prof0 = h->profiling;
+  const uint64_t substeps0 = h->substeps, launches0 = h->launches;
+  h->harvest();
+  h->profiling = true;
+  auto trial = [&](int cls) -> double {
+    h->harvest();
+    double before = h->class_ms[cls];
+    uint32_t cnt0 = h->class_count[cls];
+    for (uint32_t k = 0; k < substeps; ++k) enqueue_substep(h, CLSPH_STAGE_ADVECT);
+    cudaStreamSynchronize(h->stream);
+    h->harvest();
+    save(true);
+    h->ids_sel = ids_sel0;
+    uint32_t c = h->class_count[cls] - cnt0;
+    return c ? (h->class_ms[cls] - before) / c : 1e30;
+  };
+  std::string out;
+  const int blocks[3] = {64, 128, 256};
+  int best_d = h->density_block, best_f = h->forces_block;
+  double td = 1e30, tf = 1e30;
+  for (int b : blocks) {
+    h->density_block = b;
+    h->forces_block = b;
+    trial(K_DENSITY);  // warm-up of this shape
+    double d = trial(K_DENSITY);
+    double f = trial(K_FORCES);
+    out += "density/forces block " + std::to_string(b) + ": " + std::to_string(d) + " / " +
+           std::to_string(f) + " ms\n";
+    if (d < td) { td = d; best_d = b; }
+    if (f < tf) { tf = f; best_f = b; }
+  }
+  h->density_block = best_d;
+  h->forces_block = best_f;
+  const uint32_t advect_opts[3] = {4, 8, 16};
+  uint32_t best_a = h->advect_blocks_per_sm;
+  double ta = 1e30;
+  for (uint32_t a : advect_opts) {
+    h->advect_blocks_per_sm = a;
+    double t = trial(K_ADVECT);
+    out += "advect blocks/SM " + std::to_string(a) + ": " + std::to_string(t) + " ms\n";
+    if (t < ta) { ta = t; best_a = a; }
+  }
+  h->advect_blocks_per_sm = best_a;
+  out += "chosen: density block " + std::to_string(best_d) + ", forces block " + std::to_string(best_f) +
+         ", advect blocks/SM " + std::to_string(best_a) + "\n";
+  h->profiling = prof0;
+  for (int k = 0; k < K_NUM_CLASSES; ++k) {
+    h->class_ms[k] = 0.0;
+    h->class_count[k] = 0;
+  }
+  h->substeps = substeps0;
+  h->launches = launches0;
+  h->drop_graph();  // launch shapes changed
+  cudaStreamSynchronize(h->stream);
+  cudaFree(snap);
+  cudaFree(snap_ids);
+  cudaFree(snap_bbox);
+  if (report && report_len > 0) std::snprintf(report, report_len, "%s", out.c_str());
+  return check_launch(h);
+}
+
+int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block,
+                               uint32_t advect_blocks_per_sm) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_launch_shape: null handle");
+  auto ok = [](int b) { return b == 64 || b == 128 || b == 256; };
+  if (!ok(density_block) || !ok(forces_block) || advect_blocks_per_sm == 0 || advect_blocks_per_sm > 64)
+    return fail(CLSPH_ERR_ARGUMENT, "set_launch_shape: unsupported shape");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->density_block = density_block;
+  h->forces_block = forces_block;
+  h->advect_blocks_per_sm = advect_blocks_per_sm;
+  h->drop_graph();
   return CLSPH_OK;
 }
 

@@ -684,13 +684,14 @@ __device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint3
       }
 }
 
-__global__ void __launch_bounds__(kGatherBlock)
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
     k_density(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
               const uint32_t* __restrict__ ctl,
               const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos, CellIndex ci,
               const Consts* __restrict__ consts, float4* __restrict__ aux_out,
               uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap) {
-  __shared__ uint32_t cand[kScanCap][kGatherBlock];
+  __shared__ uint32_t cand[kScanCap][BLOCK];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const KeySplit split{ctl[kCtlShift]};
@@ -738,7 +739,8 @@ __global__ void __launch_bounds__(kGatherBlock)
 
 // Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58), walking
 // the neighbour list of k_density (or the window, for overflowing lists).
-__global__ void __launch_bounds__(kGatherBlock)
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
     k_forces(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
              const uint32_t* __restrict__ ctl,
              const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,

@@ -50,6 +50,8 @@ SIGNATURES = [
      [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _vp, _vp, ctypes.POINTER(ctypes.c_int)]),
     ("clsph_gpu_counters", ctypes.c_int, [_vp, _vp]),
     ("clsph_gpu_sort_keys_noalloc", ctypes.c_int, [_vp, _vp, _vp, _u32, _vp]),
+    ("clsph_gpu_autotune", ctypes.c_int, [_vp, _u32, ctypes.c_char_p, ctypes.c_int]),
+    ("clsph_gpu_set_launch_shape", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u32]),
     ("clsph_gpu_last_error", ctypes.c_char_p, []),
 ]
 
@@ -256,6 +258,16 @@ class GpuSolver:
             name = names.raw[i * stride:(i + 1) * stride].split(b"\0", 1)[0].decode()
             out[name] = (float(ms[i]), int(counts[i]))
         return out
+
+    def autotune(self, substeps: int = 3) -> str:
+        buf = ctypes.create_string_buffer(4096)
+        _check("clsph_gpu_autotune", self.lib.clsph_gpu_autotune(self.h, substeps, buf, 4096))
+        return buf.value.decode()
+
+    def set_launch_shape(self, density_block: int, forces_block: int, advect_blocks_per_sm: int) -> None:
+        _check("clsph_gpu_set_launch_shape",
+               self.lib.clsph_gpu_set_launch_shape(self.h, density_block, forces_block,
+                                                   advect_blocks_per_sm))
 
     def counters(self) -> dict:
         c = np.zeros(3, dtype=np.uint64)

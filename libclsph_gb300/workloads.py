@@ -160,6 +160,32 @@ def dam_break_1m(seed: int = 1) -> Scene:
     return dam_break((128, 128, 64), box=(4.0, 2.0, 2.0), seed=seed, steps=2000)
 
 
+def batched_dam_breaks(count: int = 256, seed: int = 5, n_min: int = 2048, n_max: int = 65536,
+                       steps: int = 1000) -> list:
+    """`count` independent dam breaks: particle count log-uniform in
+    [n_min, n_max], box edge 1 m * (N / 32768)^(1/3) (12 triangles), rest
+    density uniform in [900, 1200] kg/m^3, viscosity uniform in [0.5, 4] x
+    water's, m = 0.05 kg, lattice spacing h/2 with seeded jitter (the
+    32,768-particle scene scaled to each count)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        rho0 = float(rng.uniform(900.0, 1200.0))
+        mu = float(WATER["dynamic_viscosity"] * rng.uniform(0.5, 4.0))
+        st = water_settings(n, fluid_density=rho0, dynamic_viscosity=mu)
+        h = float(st.params["h"])
+        s = h / 2
+        edge = (n / 32768.0) ** (1.0 / 3.0)
+        side = int(math.ceil(n ** (1.0 / 3.0)))
+        block = lattice((side, side, side), s, (0.0, 0.0, 0.0), 0.01, rng)[:n]
+        block += np.float32((edge - side * s) / 2)  # centred in its box
+        out.append(Scene(f"batched_{k}", st.params, st.terms, particles_from_arrays(block),
+                         box_mesh((0, 0, 0), (edge, edge, edge)), steps,
+                         {"h": h, "rho0": rho0, "mu": mu, "edge": edge, "seed": seed}))
+    return out
+
+
 def pour(cross: int = 64, length: int = 1024, quads: int = 256, seed: int = 3,
          steps: int = 3000) -> Scene:
     box = (4.0, 2.0, 4.0)  # x, y (up), z
@@ -198,5 +224,6 @@ def small_block(n_side: int = 8, seed: int = 0, box=(1.0, 1.0, 1.0), offset=(0.3
 
 
 __all__ = ["Scene", "box_mesh", "heightfield_mesh", "merge_meshes", "make_mesh", "face_normals",
-           "water_settings", "mass_for_h", "dam_break", "dam_break_32k", "dam_break_1m", "pour", "small_block", "lattice",
+           "water_settings", "mass_for_h", "dam_break", "dam_break_32k", "dam_break_1m", "pour",
+           "batched_dam_breaks", "small_block", "lattice",
            "PARAMS", "PARTICLE"]

@@ -81,3 +81,36 @@ def test_graph_replay_equals_launches(gpu_lib, steps):
     assert np.array_equal(results[0][0].view(np.uint8), results[1][0].view(np.uint8))
     assert np.array_equal(results[0][1], results[1][1])
     assert results[0][2]["substeps"] == results[1][2]["substeps"] == 2 * steps
+
+
+def test_autotune_keeps_state_and_results(gpu_lib):
+    sc = W.small_block(16, seed=80, velocity_sigma=0.3)
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.upload(sc.particles)
+        g.step(2)
+        report = g.autotune(2)
+        g.step(3)
+        tuned = g.download()
+        tuned_ids = g.ids()
+    assert "chosen:" in report
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.upload(sc.particles)
+        g.step(5)
+        plain = g.download()
+        plain_ids = g.ids()
+    assert np.array_equal(tuned.view(np.uint8), plain.view(np.uint8))
+    assert np.array_equal(tuned_ids, plain_ids)
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 4), (256, 256, 16)])
+def test_launch_shapes_do_not_change_results(gpu_lib, shape):
+    sc = W.small_block(15, seed=81, velocity_sigma=0.3)
+    outs = []
+    for sh in (None, shape):
+        with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+            if sh:
+                g.set_launch_shape(*sh)
+            g.upload(sc.particles)
+            g.step(4)
+            outs.append(g.download())
+    assert np.array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
