@@ -19,6 +19,7 @@
 #ifndef _SPH_SIMULATION_H_
 #define _SPH_SIMULATION_H_
 
+#include <cstring>
 #include <functional>
 #include <string>
 
@@ -29,7 +30,11 @@ struct clsph_gpu;
 
 class sph_simulation {
  public:
-  sph_simulation() : parameters(), write_intermediate_frames(false) {}
+  // Padding bytes of the parameter block are zeroed too, so that copies of it
+  // (callbacks, the C ABI) are byte-for-byte reproducible.
+  sph_simulation() : parameters(), write_intermediate_frames(false) {
+    std::memset(&parameters, 0, sizeof(parameters));
+  }
   ~sph_simulation();
   sph_simulation(const sph_simulation&) = delete;
   sph_simulation& operator=(const sph_simulation&) = delete;

@@ -1,5 +1,5 @@
 // Raw binary archives with the two calls libclsph uses for last_frame.bin
-// (example/particles.cpp:40-44 saveBinary, sph_simulation.cpp:114-121
+// (example/particles.cpp:40-44 saveBinary, sph_simulation.cpp:60-67
 // loadBinary): the bytes of the particle AoS, no header. A minimal stand-in
 // for the vendored cereal binary archive so that code written against the
 // reference compiles unchanged.

@@ -11,7 +11,7 @@
  *   clsph_kernel_terms = precomputed_kernel_values   (structures.h:48-54), 20 B
  *
  * One call of clsph_gpu_step(h, 1) is one call of the reference's
- * sph_simulation::simulate_single_frame (libclsph/sph_simulation.cpp:227-398):
+ * sph_simulation::simulate_single_frame (libclsph/sph_simulation.cpp:173-344):
  * bounding box + grid, Morton keys, stable sort, cell offsets, density and
  * Tait pressure, internal forces, leapfrog + mesh collision. Particles stay
  * resident in device memory between substeps; host transfers happen only in
@@ -61,7 +61,7 @@ typedef struct clsph_gpu clsph_gpu;
 enum {
   CLSPH_OK = 0,
   CLSPH_WARN_GRID_OVERFLOW = 1,  /* a grid axis reached 1024 cells: keys wrap
-                                    (the reference asserts, sph_simulation.cpp:301-303) */
+                                    (the reference asserts, sph_simulation.cpp:247-249) */
   CLSPH_WARN_COLLISION_CAP = 2,  /* an advect/collide loop hit its iteration cap
                                     (the reference loop is unbounded, sph.cl:82-101) */
   CLSPH_WARN_NONFINITE = 4,      /* a non-finite position was seen */
@@ -82,10 +82,10 @@ enum {
 };
 
 /* Replaces the context/queue/program/buffer set-up of sph_simulation::simulate
- * (sph_simulation.cpp:400-434). Allocates all device memory for up to n
+ * (sph_simulation.cpp:346-380). Allocates all device memory for up to n
  * particles on the current CUDA device; no allocation happens per substep.
  * params: the derived parameter block of sph_simulation::load_settings
- * (sph_simulation.cpp:459-559); particles_count is replaced by n. */
+ * (sph_simulation.cpp:405-505); particles_count is replaced by n. */
 int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* terms, uint32_t n,
                      clsph_gpu** out);
 
@@ -109,7 +109,7 @@ int clsph_gpu_set_collision_cap(clsph_gpu* h, uint32_t max_iterations);
 /* Launch stream (a cudaStream_t); NULL selects the handle's own stream. */
 int clsph_gpu_set_stream(clsph_gpu* h, void* cuda_stream);
 
-/* Replaces the per-substep mesh buffers of sph_simulation.cpp:350-373: the
+/* Replaces the per-substep mesh buffers of sph_simulation.cpp:296-319: the
  * scene (scene.h:11-14 arrays) is uploaded once and indexed by a per-cell
  * triangle list. Face order is kept, so hit selection equals the reference's
  * brute-force loop (collisions.cl:21-87). */
@@ -126,18 +126,18 @@ int clsph_gpu_set_scene_mesh(clsph_gpu* h, uint32_t scene, const float* face_nor
  * it is bypassed while profiling. */
 int clsph_gpu_set_graph(clsph_gpu* h, int enabled);
 
-/* Replaces the enqueueWriteBuffer of sph_simulation.cpp:249-251: host AoS ->
+/* Replaces the enqueueWriteBuffer of sph_simulation.cpp:195-197: host AoS ->
  * device. `particles` points to n clsph_particle (only position, velocity and
  * intermediate_velocity are read, as in the reference). */
 int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles);
 
-/* Replaces the enqueueReadBuffer of sph_simulation.cpp:393-395: device -> host
+/* Replaces the enqueueReadBuffer of sph_simulation.cpp:339-341: device -> host
  * AoS in the current (sorted) order, with density, pressure and grid_index of
  * the last substep and acceleration = 0, as the reference leaves them.
  * Synchronises the stream. */
 int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles);
 
-/* `substeps` calls of simulate_single_frame (sph_simulation.cpp:227-398) with
+/* `substeps` calls of simulate_single_frame (sph_simulation.cpp:173-344) with
  * no host round trip in between. Asynchronous on the handle's stream. */
 int clsph_gpu_step(clsph_gpu* h, uint32_t substeps);
 
@@ -158,7 +158,7 @@ int clsph_gpu_get_scene_parameters(clsph_gpu* h, uint32_t scene, clsph_parameter
  * key) per slot; perm: sorted slot -> slot before the sort (may be NULL). */
 int clsph_gpu_read_keys(clsph_gpu* h, uint32_t* keys, uint32_t* perm);
 
-/* The reference's dense cell table (sph_simulation.cpp:216-224) rebuilt from
+/* The reference's dense cell table (sph_simulation.cpp:162-170) rebuilt from
  * the device cell index: table[c] = first sorted slot with key >= c, for
  * c < grid_cell_count. Needs cap >= grid_cell_count. Debug path: allocates. */
 int clsph_gpu_read_cell_table(clsph_gpu* h, uint32_t* table, uint64_t cap);

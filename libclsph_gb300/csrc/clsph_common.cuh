@@ -34,7 +34,7 @@ __device__ __forceinline__ float xdot(V3 a, V3 b) {
 __device__ __forceinline__ V3 v3(float4 f) { return {f.x, f.y, f.z}; }
 
 // ---------------------------------------------------------------- Morton
-// 10 bits per axis; x -> bit 3k, y -> 3k+1, z -> 3k+2 (libclsph/common/util.h:97-118).
+// 10 bits per axis; x -> bit 3k, y -> 3k+1, z -> 3k+2 (libclsph/common/util.h:41-62).
 // Bit spreading by the standard shift-and-mask sequence ("Part1By2").
 __host__ __device__ __forceinline__ uint32_t spread_bits3(uint32_t v) {
   v &= 0x3FFu;

@@ -178,7 +178,7 @@ __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const
 
 // --------------------------------------------------------------- kernels
 
-// Grid set-up of every scene (sph_simulation.cpp:253-306), one thread per
+// Grid set-up of every scene (sph_simulation.cpp:199-252), one thread per
 // scene, from the bounding boxes accumulated by the previous kernel; resets
 // the boxes, the radix digit totals and the sort control for this substep.
 __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
@@ -218,7 +218,7 @@ __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restric
   for (int i = 0; i < 4; ++i) g.pad_[i] = 0u;
   *grid = g;
   if (overflow) atomicOr(status, kFlagGridOverflow);
-  // sentinels of sph_simulation.cpp:258-259 for the next accumulation
+  // sentinels of sph_simulation.cpp:204-205 for the next accumulation
   for (int a = 0; a < 3; ++a) {
     bbox[a] = f2ord(2147483648.0f);
     bbox[3 + a] = f2ord(-2147483648.0f);
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(kRadixThreads)
 
 // Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
 // and records every cell's [start, end) in the cell index (the dense cell
-// table of sph_simulation.cpp:216-224 in compact form).
+// table of sph_simulation.cpp:162-170 in compact form).
 __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
                          const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
                          const uint32_t* __restrict__ keys_base,

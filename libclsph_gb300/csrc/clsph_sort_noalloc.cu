@@ -6,7 +6,7 @@
 // synchronisation would stall its other work), or a fixed-budget real-time
 // loop that must not allocate after start-up. This entry point runs the
 // substep's stable sort (the 4 x 8-bit LSD radix sort of
-// libclsph/sph_simulation.cpp:161-210 + kernels/sort.cl, with 32-bit offsets)
+// libclsph/sph_simulation.cpp:107-156 + kernels/sort.cl, with 32-bit offsets)
 // on caller-provided device buffers and takes its scratch space from one
 // file-scope __device__ array instead of cudaMalloc.
 //

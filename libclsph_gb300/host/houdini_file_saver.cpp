@@ -15,7 +15,7 @@
 
 namespace {
 
-// Last 7 digits of the zero-padded counter (houdini_file_saver.cpp:12-23).
+// Last 7 digits of the zero-padded counter (houdini_file_saver.cpp:15-23).
 std::string frame_number(int num) {
   std::ostringstream ss;
   ss << std::setw(9) << std::setfill('0') << num;

@@ -1,7 +1,7 @@
 // Minimal JSON reader for libclsph's property files (fluid_properties/*.json,
 // simulation_properties/*.json). Reads the first JSON value of a stream and
 // ignores what follows it (the files end with `};`), like the stream parse of
-// the picojson the reference uses in sph_simulation.cpp:463-542.
+// the picojson the reference uses in sph_simulation.cpp:409-488.
 #pragma once
 
 #include <istream>

@@ -1,6 +1,6 @@
 // scene::load (libclsph/scene.cpp:9-67) with an OBJ reader that gives the
 // same arrays as the tinyobjloader 0.9.6 the reference vendors
-// (util/tinyobj/tiny_obj_loader.cc:461-718):
+// (util/tinyobj/tiny_obj_loader.cc:118-661):
 //   * v / vn / vt records read with atof, f records of i, i/j, i//k, i/j/k
 //     with 1-based or negative (relative) indices;
 //   * polygons become the triangle fan (v0, v[k-1], v[k]);

@@ -1,10 +1,10 @@
 // sph_simulation (libclsph/sph_simulation.h:8-52) on the GB300 engine.
 //
-//   load_settings  libclsph/sph_simulation.cpp:459-559 (JSON + derived values)
-//   init_particles sph_simulation.cpp:102-148 (last_frame.bin or cube lattice)
-//   simulate       sph_simulation.cpp:400-457 (frames x substeps + callbacks)
+//   load_settings  libclsph/sph_simulation.cpp:405-505 (JSON + derived values)
+//   init_particles sph_simulation.cpp:48-94 (last_frame.bin or cube lattice)
+//   simulate       sph_simulation.cpp:346-403 (frames x substeps + callbacks)
 // Each substep is clsph_gpu_step(h, 1), the whole of simulate_single_frame
-// (sph_simulation.cpp:227-398) on the device. Errors that the reference turns
+// (sph_simulation.cpp:173-344) on the device. Errors that the reference turns
 // into exit(-1) or assert() are thrown as std::runtime_error.
 
 #include <cmath>
@@ -83,7 +83,7 @@ void sph_simulation::load_settings(std::string fluid_file_name, std::string para
     write_intermediate_frames = s.at("write_all_frames").as_bool("write_all_frames");
     serialize = s.at("serialize").as_bool("serialize");
   }
-  // derived values (sph_simulation.cpp:544-559): float arithmetic, except the
+  // derived values (sph_simulation.cpp:490-505): float arithmetic, except the
   // division by 4*pi and the kernel constants, which the reference evaluates
   // in double (M_PI and ::pow are double) before narrowing.
   parameters.total_mass = parameters.particles_count * parameters.particle_mass;
@@ -133,7 +133,7 @@ void sph_simulation::simulate(int frame_count) {
         "clsph_gpu_create");
   check(clsph_gpu_set_collision_cap(gpu_, collision_iteration_cap), "clsph_gpu_set_collision_cap");
   // The reference hands face_normals.data() with face_count faces to the
-  // kernel (sph_simulation.cpp:350-391): the first face_count normals.
+  // kernel (sph_simulation.cpp:296-337): the first face_count normals.
   if (current_scene.face_count > 0) {
     if (current_scene.face_normals.size() < 3ull * current_scene.face_count ||
         current_scene.indices.size() < 3ull * current_scene.face_count)

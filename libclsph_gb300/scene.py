@@ -3,7 +3,7 @@
 `Scene.load(filename)` reads `scenes/<filename>` (relative to the working
 directory, like the reference; `base` overrides the folder) with the same
 geometry semantics as the vendored tinyobjloader 0.9.6 the reference uses
-(util/tinyobj/tiny_obj_loader.cc:461-718):
+(util/tinyobj/tiny_obj_loader.cc:118-661):
 
 * `v`/`vn`/`vt` records parsed with C `atof` (longest numeric prefix),
 * `f` records of `i`, `i/j`, `i//k`, `i/j/k` with 1-based or negative

@@ -1,6 +1,6 @@
 """Fluid / simulation property files and the derived parameter block.
 
-Mirrors `sph_simulation::load_settings` (libclsph/sph_simulation.cpp:459-559):
+Mirrors `sph_simulation::load_settings` (libclsph/sph_simulation.cpp:405-505):
 the two JSON files (fluid_properties/*.json, simulation_properties/*.json,
 whose objects end with `};`), the restitution range check, and the derived
 h, time_delta, max_velocity and the five smoothing-kernel constants with the
@@ -66,7 +66,7 @@ class Settings:
 
 
 def derive(params: np.void, influence_count: int) -> tuple[np.void, np.void, float]:
-    """Derived fields of sph_simulation.cpp:544-559 (see module docstring)."""
+    """Derived fields of sph_simulation.cpp:490-505 (see module docstring)."""
     p = np.array(params, dtype=PARAMS).reshape(1).copy()
     n = int(p["particles_count"][0])
     m = f32(p["particle_mass"][0])
@@ -97,7 +97,7 @@ def settings_from_dicts(fluid: dict, sim: dict) -> Settings:
     p["fluid_density"] = float(fluid["fluid_density"])
     p["dynamic_viscosity"] = float(fluid["dynamic_viscosity"])
     restitution = f32(float(fluid["restitution"]))
-    if restitution < 0 or restitution > 1:  # sph_simulation.cpp:477-479
+    if restitution < 0 or restitution > 1:  # sph_simulation.cpp:423-425
         raise ValueError("Restitution has an invalid value!")
     p["restitution"] = restitution
     p["K"] = float(fluid["k"])

@@ -32,7 +32,7 @@ FRAMES_ONLY = "frames_only"
 
 
 def init_lattice(n: int, initial_volume: float) -> np.ndarray:
-    """sph_simulation.cpp:102-148 cube lattice (no last_frame.bin)."""
+    """sph_simulation.cpp:48-94 cube lattice (no last_frame.bin)."""
     side = int(math.ceil(float(cbrtf(n))))
     length = cbrtf(initial_volume)
     gap = f32(length / f32(side))

@@ -42,7 +42,7 @@ class Scene:
 
 
 def face_normals(vertices: np.ndarray, indices: np.ndarray) -> np.ndarray:
-    """Unit normals from the cross product (libclsph/scene.cpp:51-80), float32."""
+    """Unit normals from the cross product (libclsph/scene.cpp:35-64), float32."""
     v = np.asarray(vertices, dtype=np.float32).reshape(-1, 3)
     t = v[np.asarray(indices, dtype=np.int64).reshape(-1, 3)]
     u = (t[:, 1] - t[:, 0]).astype(np.float32)

@@ -5,16 +5,16 @@
 // (libclsph_gb300) never links or calls it.
 //
 // It restates, in its own code, what the reference computes for one substep:
-//   bounding box + grid        libclsph/sph_simulation.cpp:253-306
-//   Morton cell key            libclsph/common/util.h:60-118, kernels/grid.cl:43-67
-//   stable sort + cell table   libclsph/sph_simulation.cpp:161-225, kernels/sort.cl:1-59
+//   bounding box + grid        libclsph/sph_simulation.cpp:199-252
+//   Morton cell key            libclsph/common/util.h:4-62, kernels/grid.cl:43-67
+//   stable sort + cell table   libclsph/sph_simulation.cpp:107-171, kernels/sort.cl:1-59
 //   smoothing kernels          libclsph/kernels/smoothing.cl:1-34
 //   density + Tait pressure    kernels/forces.cl:15-43, kernels/sph.cl:9-40
 //   internal forces            kernels/forces.cl:45-112, kernels/sph.cl:42-62
 //   leapfrog + mesh collision  kernels/advection.cl:6-23, kernels/collisions.cl:15-129,
 //                              kernels/sph.cl:64-112
-//   parameter derivation       libclsph/sph_simulation.cpp:544-559
-//   initial lattice            libclsph/sph_simulation.cpp:102-148
+//   parameter derivation       libclsph/sph_simulation.cpp:490-505
+//   initial lattice            libclsph/sph_simulation.cpp:48-94
 //
 // Single precision follows the reference's expression order operation by
 // operation with plain IEEE float arithmetic (built with -ffp-contract=off),
@@ -75,7 +75,7 @@ static_assert(offsetof(Params, gx) == 80, "parameter layout");
 static_assert(offsetof(Params, min_point) == 96, "parameter layout");
 
 // ---------------------------------------------------------------- Morton keys
-// 10 bits per axis, x in bit 3k, y in 3k+1, z in 3k+2 (util.h:97-118).
+// 10 bits per axis, x in bit 3k, y in 3k+1, z in 3k+2 (util.h:41-62).
 uint32_t spread10(uint32_t v) {
   uint32_t out = 0;
   for (int b = 0; b < 10; ++b) out |= ((v >> b) & 1u) << (3 * b);
@@ -401,7 +401,7 @@ int step_impl(Params& p, const Terms& terms, const float* fn, const float* vx, c
               void* snap_forces, uint32_t max_iters, uint32_t* capped_out, int threads) {
   p.n = n;
   const int nt = resolve_threads(threads);
-  // bounding box (sph_simulation.cpp:253-271): `<`/`>` comparisons skip NaN
+  // bounding box (sph_simulation.cpp:199-217): `<`/`>` comparisons skip NaN
   const float cell = p.h * 2;
   float lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
@@ -438,7 +438,7 @@ int step_impl(Params& p, const Terms& terms, const float* fn, const float* vx, c
   }
 
   // stable counting sort over the dense cell range; the exclusive prefix sum of
-  // the counts is the reference's cell table (sph_simulation.cpp:216-224)
+  // the counts is the reference's cell table (sph_simulation.cpp:162-170)
   std::vector<uint32_t> table((size_t)p.cell_count + 1, 0u);
   std::vector<uint32_t> perm(n);
   {

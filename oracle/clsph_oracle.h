@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-/* One substep (sph_simulation.cpp:227-398). Status: 0 ok, 1 bad argument,
+/* One substep (sph_simulation.cpp:173-344). Status: 0 ok, 1 bad argument,
  * 2 grid >= 1024 cells on an axis, 3 cell_table_out too small.
  * particles_io: in = host AoS, out = AoS after the substep (sorted order).
  * Optional outputs (NULL to skip): params_out (grid fields filled),
@@ -50,13 +50,13 @@ int clsph_oracle_fields_f64(const void* params, const void* sorted_aos, uint32_t
                             const uint32_t* cell_table, double* density, double* pressure,
                             double* accel, int threads);
 
-/* sph_simulation.cpp:544-559: derived parameters from the JSON numbers.
+/* sph_simulation.cpp:490-505: derived parameters from the JSON numbers.
  * params_io has the JSON fields filled; h, time_delta, max_velocity,
  * total_mass are written, terms_out gets the 5 kernel constants. */
 void clsph_oracle_derive(void* params_io, void* terms_out, int particles_inside_influence_radius,
                          float* initial_volume_out);
 
-/* sph_simulation.cpp:102-148 cube lattice used when no last_frame.bin exists. */
+/* sph_simulation.cpp:48-94 cube lattice used when no last_frame.bin exists. */
 void clsph_oracle_init_lattice(void* particles_out, uint32_t n, float initial_volume);
 
 uint32_t clsph_oracle_morton(uint32_t x, uint32_t y, uint32_t z);

@@ -3,9 +3,9 @@
 // plus a restatement of the parts that cannot compile as C++:
 //   * the three kernel bodies of libclsph/kernels/sph.cl:9-112 (they use
 //     OpenCL work-group built-ins), and
-//   * the host orchestration of libclsph/sph_simulation.cpp:227-398
+//   * the host orchestration of libclsph/sph_simulation.cpp:173-344
 //     (it is written against cl.hpp), including the 4-pass / 128-chunk LSD
-//     radix sort of sph_simulation.cpp:161-225 + kernels/sort.cl:1-59 with
+//     radix sort of sph_simulation.cpp:107-171 + kernels/sort.cl:1-59 with
 //     32-bit offsets (the intended behaviour; sort.cl:42 reads the offsets
 //     through a size_t pointer, which is a bug on 64-bit devices).
 //
@@ -110,7 +110,7 @@ static_assert(sizeof(simulation_parameters) == 128, "parameter block must be 128
 static_assert(offsetof(particle, density) == 64, "density offset");
 static_assert(offsetof(particle, grid_index) == 72, "grid_index offset");
 
-// sph_simulation.cpp:161-210: 4 passes x 8-bit digits, 128 contiguous chunks,
+// sph_simulation.cpp:107-156: 4 passes x 8-bit digits, 128 contiguous chunks,
 // bucket-major exclusive scan -> stable LSD radix sort. Applied to an index
 // array so that the permutation can be reported.
 static void ref_radix_sort(const particle* in, particle* out, uint32_t* perm, uint32_t n) {
@@ -158,7 +158,7 @@ static void ref_radix_sort(const particle* in, particle* out, uint32_t* perm, ui
 extern "C" {
 
 // Return codes shared with the oracle: 0 ok, 1 bad argument, 2 grid >= 1024
-// cells on an axis (sph_simulation.cpp:301-303 asserts), 3 cell table too
+// cells on an axis (sph_simulation.cpp:247-249 asserts), 3 cell table too
 // small for the caller's buffer.
 int clsph_ref_step(const void* params_in, void* params_out, const void* terms_in,
                    const float* normals, const float* vertices, const uint32_t* indices,
@@ -174,7 +174,7 @@ int clsph_ref_step(const void* params_in, void* params_out, const void* terms_in
   params.particles_count = n;
   particle* host = static_cast<particle*>(particles_io);
 
-  // sph_simulation.cpp:253-306 bounding box, padding, grid dimensions
+  // sph_simulation.cpp:199-252 bounding box, padding, grid dimensions
   float cell = params.h * 2;
   float mnx, mny, mnz, mxx, mxy, mxz;
   mnx = mny = mnz = (float)std::numeric_limits<int>::max();
@@ -211,7 +211,7 @@ int clsph_ref_step(const void* params_in, void* params_out, const void* terms_in
   ref_radix_sort(back.data(), front.data(), perm_out, n);
   if (snap_sorted) std::memcpy(snap_sorted, front.data(), sizeof(particle) * n);
 
-  // sph_simulation.cpp:216-224 dense cell table
+  // sph_simulation.cpp:162-170 dense cell table
   std::vector<unsigned int> table(params.grid_cell_count);
   {
     unsigned int at = 0;

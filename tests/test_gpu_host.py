@@ -1,6 +1,6 @@
 """The reference-compatible host layer on the GPU: the Python Simulation mirror
 and the C++ sph_simulation (through a drop-in example program) run the same
-frames/substeps/callbacks loop as libclsph/sph_simulation.cpp:400-457."""
+frames/substeps/callbacks loop as libclsph/sph_simulation.cpp:346-403."""
 
 import json
 import os

@@ -72,7 +72,7 @@ def test_derived_parameters_match_oracle_and_cpp(tmp_path, oracle, host, fluid, 
     sim = dict(S.DEFAULT_SIM, particles_count=n)
     f, s = write_props(tmp_path, fluid, sim)
     st = S.load_settings(f, s)
-    # oracle restatement of sph_simulation.cpp:544-559
+    # oracle restatement of sph_simulation.cpp:490-505
     raw = np.zeros(1, dtype=PARAMS)[0]
     for k in PARAMS.names:
         raw[k] = st.params[k]
