@@ -307,6 +307,35 @@ def run_reference(args, world, rank) -> None:
     print(json.dumps(line), flush=True)
 
 
+def learned_evaluation(scene, solver) -> dict | None:
+    """Plain vs learned 4x-dt over the time of 2000 plain substeps (weights
+    from libclsph_gb300/weights/stepper_4dt.npz; skipped when absent)."""
+    from libclsph_gb300 import learned as Lm
+    from libclsph_gb300.stepper_eval import evaluate
+
+    path = Lm.default_weights_path()
+    if not path.exists():
+        return {"skipped": f"no weights at {path.relative_to(ROOT)}"}
+    import torch
+
+    mlp = Lm.Mlp.load(path)
+    solver.set_graph(False)
+    torch.cuda.synchronize()
+    r = evaluate(scene, mlp, plain_substeps=2000, dt_mult=4, checkpoints=10, threshold=0.01)
+    mlp.close()
+    keep = ("plain_sim_s_per_s", "learned_sim_s_per_s", "speedup", "fallback_fraction", "accepted_steps",
+            "rejected_steps", "check_deviation_mean", "check_deviation_max", "density_dev_mean",
+            "density_dev_pop", "density_dev_mean_final", "pos_rms_h_final", "threshold", "dt_mult",
+            "plain_substeps", "learned_steps", "sim_time_s")
+    out = {k: r[k] for k in keep}
+    out["curve_t"] = [c["t"] for c in r["curve"]]
+    out["curve_density_dev_mean"] = [c["density_dev_mean"] for c in r["curve"]]
+    out["curve_pos_rms_h"] = [c["pos_rms_h"] for c in r["curve"]]
+    out["curve_ke_plain"] = [c["ke_plain"] for c in r["curve"]]
+    out["curve_ke_learned"] = [c["ke_learned"] for c in r["curve"]]
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,6 +348,8 @@ def main() -> None:
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch every kernel instead of replaying a CUDA graph")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned 4x-dt stepper's evaluation on the 1M dam break")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -423,6 +454,11 @@ def main() -> None:
             traffic = None
     step_achieved = STEP_ALG_BYTES * n * args.steps / device_s / 1e9
 
+    # ---- learned 4x-dt stepper against the plain solver (the 1M dam break only)
+    learned = None
+    if not args.no_learned and args.workload == "dam_break_1m":
+        learned = learned_evaluation(scene, solver)
+
     if rank != 0:
         return
     cpu = None
@@ -478,6 +514,7 @@ def main() -> None:
         "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": n * PARTICLE.itemsize,
                 "d2h_bytes_per_step": n * PARTICLE.itemsize, "steps": args.e2e_steps},
+        "learned": learned,
         "gpu_launches": launches,
         "device_flags": flags,
         "clocks": clocks.summary(),

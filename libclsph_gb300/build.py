@@ -44,12 +44,22 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed: {' '.join(cmd[:3])} ...")
 
 
-def gpu_cmd(extra: list[str] | None = None) -> list[str]:
-    srcs = [str(CSRC / "clsph_gpu.cu"), str(CSRC / "clsph_sort_noalloc.cu")]
+GPU_SOURCES = ["clsph_gpu.cu", "clsph_sort_noalloc.cu", "clsph_learned.cu"]
+OBJ_DIR = LIB_DIR / "obj"
+
+
+def gpu_compile_cmd(src: str, extra: list[str] | None = None) -> list[str]:
+    """nvcc command compiling one translation unit of the engine to an object."""
     return [
-        _nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-        f"-I{INCLUDE}", f"-I{CSRC}", *(extra or []), "-o", str(GPU_SO), *srcs,
+        _nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+        f"-I{INCLUDE}", f"-I{CSRC}", *(extra or []), "-o", str(OBJ_DIR / (Path(src).stem + ".o")),
+        str(CSRC / src),
     ]
+
+
+def gpu_link_cmd() -> list[str]:
+    return [_nvcc(), *ARCH, "-shared", "-o", str(GPU_SO),
+            *[str(OBJ_DIR / (Path(src).stem + ".o")) for src in GPU_SOURCES]]
 
 
 def host_cmd() -> list[str]:
@@ -72,8 +82,11 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 def build_gpu(force: bool = False) -> Path:
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
     if force or _stale(GPU_SO, deps):
-        LIB_DIR.mkdir(exist_ok=True)
-        _run(gpu_cmd())
+        OBJ_DIR.mkdir(parents=True, exist_ok=True)
+        with ThreadPoolExecutor(max_workers=len(GPU_SOURCES)) as ex:
+            for f in [ex.submit(_run, gpu_compile_cmd(src)) for src in GPU_SOURCES]:
+                f.result()
+        _run(gpu_link_cmd())
     return GPU_SO
 
 

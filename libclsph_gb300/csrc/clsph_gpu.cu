@@ -16,9 +16,7 @@
 #include <vector>
 
 #include "clsph_gpu.h"
-#include "clsph_kernels.cuh"
-
-using namespace clsph;
+#include "clsph_handle.cuh"
 
 static_assert(sizeof(clsph_particle) == 80, "particle layout");
 static_assert(sizeof(clsph_parameters) == 128, "parameter layout");
@@ -27,7 +25,7 @@ static_assert(offsetof(clsph_parameters, grid_size_x) == 80, "parameter layout")
 static_assert(offsetof(clsph_parameters, min_point) == 96, "parameter layout");
 static_assert(sizeof(clsph_kernel_terms) == 20, "kernel constant layout");
 
-namespace {
+namespace clsph_host {
 
 thread_local std::string g_last_error;
 
@@ -36,198 +34,15 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-#define CUDA_TRY(expr)                                                                  \
-  do {                                                                                  \
-    cudaError_t err_ = (expr);                                                          \
-    if (err_ != cudaSuccess)                                                            \
-      return fail(CLSPH_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(err_)); \
-  } while (0)
-
-enum KernelClass {
-  K_GRID_SETUP,
-  K_KEYS,
-  K_RADIX_COUNT,
-  K_RADIX_SCAN,
-  K_RADIX_SCATTER,
-  K_GATHER,
-  K_DENSITY,
-  K_FORCES,
-  K_ADVECT,
-  K_UNPACK,
-  K_PACK,
-  K_MISC,
-  K_NUM_CLASSES
-};
-
 const char* kKernelNames[K_NUM_CLASSES] = {
-    "grid_setup", "keys", "radix_count", "radix_scan", "radix_scatter", "gather",
-    "density",    "forces", "advect",   "unpack_aos", "pack_aos",      "misc"};
+    "grid_setup", "keys",       "radix_count", "radix_scan",     "radix_scatter", "gather",
+    "density",    "forces",     "advect",      "unpack_aos",     "pack_aos",      "misc",
+    "features",   "mlp",        "learned_advect", "gate"};
 
-// kernels enqueued by one full substep (4 radix passes x 3 kernels)
-constexpr uint32_t kLaunchesPerSubstep = 2 + 12 + 4;
-
-struct PendingTiming {
-  int cls;
-  cudaEvent_t start, stop;
-};
-
-template <typename T>
-int dev_alloc(T** p, size_t count) {
-  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
-  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-  return 0;
-}
-
-uint32_t grid_blocks(uint32_t n, uint32_t cap = 0) {
-  uint32_t b = (n + kBlock - 1) / kBlock;
-  if (b == 0) b = 1;
-  if (cap && b > cap) b = cap;
-  return b;
-}
-
-float pown_f(float x, int k) {
-  float r = x;
-  for (int i = 1; i < k; ++i) r = r * x;
-  return r;
-}
-
-// Device buffers of one scene's mesh.
-struct SceneMesh {
-  float* normals = nullptr;
-  float* vertices = nullptr;
-  uint32_t* indices = nullptr;
-  uint32_t* cell_start = nullptr;
-  uint32_t* cell_faces = nullptr;
-  void release() {
-    cudaFree(normals);
-    cudaFree(vertices);
-    cudaFree(indices);
-    cudaFree(cell_start);
-    cudaFree(cell_faces);
-    *this = SceneMesh{};
-  }
-};
-
-}  // namespace
+}  // namespace clsph_host
 
 // Error text for clsph_gpu_last_error from the library's other translation units.
-void clsph_set_last_error(const std::string& msg) { g_last_error = msg; }
-
-struct clsph_gpu {
-  int device = 0;
-  uint32_t sm_count = 152;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  uint32_t n = 0;
-
-  // scenes
-  uint32_t nscenes = 1;
-  std::vector<uint32_t> scene_first;  // nscenes + 1 slot offsets
-  std::vector<clsph_parameters> params;
-  std::vector<clsph_kernel_terms> terms;
-  std::vector<Consts> consts_host;
-  std::vector<SceneMesh> scene_mesh;
-  std::vector<DevMesh> mesh_host;
-  uint16_t* scene_of = nullptr;
-  DevGrid* grids = nullptr;
-  Consts* consts = nullptr;
-  float* scene_h = nullptr;
-  DevMesh* meshes = nullptr;
-  uint32_t* bbox = nullptr;  // 6 per scene
-  uint32_t* ctl = nullptr;   // kCtlWords
-
-  State st[2]{};
-  uint32_t* ids[2]{};
-  int ids_sel = 0;
-  float4* aux = nullptr;  // (rho, p, m/rho, p/rho^2)
-  float4* acc = nullptr;
-  uint32_t* nlist = nullptr;
-  uint32_t* ncount = nullptr;
-  uint32_t nlist_cap = 64;
-  uint32_t* cell_list = nullptr;      // first sorted slot of every occupied cell
-  uint32_t* step_counters = nullptr;  // kStepCounters, zeroed every substep
-  uint32_t* keys = nullptr;           // [2n]
-  uint32_t* vals = nullptr;           // [2n]
-  uint32_t* tile_hist = nullptr;
-  uint32_t ntiles = 0;
-  uint32_t* digit_total = nullptr;
-  CellIndex ci{};
-  uint32_t slots = 0;
-  uint32_t* status = nullptr;
-  unsigned long long* capped = nullptr;
-  float4* aos_stage = nullptr;
-
-  // launch shapes chosen by clsph_gpu_autotune
-  int density_block = 128;
-  int forces_block = 128;
-  uint32_t advect_blocks_per_sm = 8;
-
-  bool uploaded = false;
-  bool partial = false;
-  bool have_fields = false;
-  uint32_t max_iters = 1024;
-
-  // CUDA graphs of two substeps, one per buffer the particle ids start in
-  bool use_graph = false;
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
-  uint32_t graph_max_iters[2] = {0, 0};
-
-  bool profiling = false;
-  std::vector<PendingTiming> pending;
-  std::vector<cudaEvent_t> event_pool;
-  double class_ms[K_NUM_CLASSES] = {};
-  uint32_t class_count[K_NUM_CLASSES] = {};
-  uint64_t substeps = 0;
-  uint64_t launches = 0;
-
-  cudaEvent_t take_event() {
-    if (!event_pool.empty()) {
-      cudaEvent_t e = event_pool.back();
-      event_pool.pop_back();
-      return e;
-    }
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    return e;
-  }
-
-  template <typename Kernel, typename... Args>
-  void launch(int cls, Kernel k, dim3 g, dim3 b, Args... args) {
-    PendingTiming t{cls, nullptr, nullptr};
-    if (profiling) {
-      t.start = take_event();
-      cudaEventRecord(t.start, stream);
-    }
-    k<<<g, b, 0, stream>>>(args...);
-    ++launches;
-    if (profiling) {
-      t.stop = take_event();
-      cudaEventRecord(t.stop, stream);
-      pending.push_back(t);
-    }
-  }
-
-  void harvest() {
-    for (auto& t : pending) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, t.start, t.stop) == cudaSuccess) {
-        class_ms[t.cls] += ms;
-        class_count[t.cls] += 1;
-      }
-      event_pool.push_back(t.start);
-      event_pool.push_back(t.stop);
-    }
-    pending.clear();
-  }
-
-  void drop_graph() {
-    for (auto& g : graph_exec) {
-      if (g) cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
-  }
-};
-
+void clsph_set_last_error(const std::string& msg) { clsph_host::g_last_error = msg; }
 namespace {
 
 Consts derive_consts(const clsph_parameters& p, const clsph_kernel_terms& t, uint32_t n) {
@@ -258,7 +73,9 @@ Consts derive_consts(const clsph_parameters& p, const clsph_kernel_terms& t, uin
   return c;
 }
 
-int enqueue_substep(clsph_gpu* h, int until) {
+}  // namespace
+
+int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   const uint32_t n = h->n;
   const uint32_t blocks = grid_blocks(n);
   const uint32_t* cctl = h->ctl;
@@ -305,26 +122,34 @@ int enqueue_substep(clsph_gpu* h, int until) {
       h->launch(K_FORCES, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
                 (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-                (const uint32_t*)h->ncount, h->nlist_cap, h->acc);
+                (const uint32_t*)h->ncount, h->nlist_cap, h->acc, NoForceHook{});
     };
     if (b == 64) args(k_forces<64>);
     else if (b == 256) args(k_forces<256>);
     else args(k_forces<128>);
   }
   if (until <= CLSPH_STAGE_FORCES) return 0;
-  h->launch(K_ADVECT, k_advect, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
+  return enqueue_advect(h);
+}
+
+int clsph_host::enqueue_advect(clsph_gpu* h) {
+  const uint32_t n = h->n;
+  h->launch(K_ADVECT, k_advect<false>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
             dim3(kBlock), n, h->st[1],
             (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes, (const Consts*)h->consts,
-            (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status, h->capped);
+            (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status, h->capped,
+            (const float4*)nullptr, 1.f, 1.f);
   return 0;
 }
 
-int check_launch(clsph_gpu* h) {
+int clsph_host::check_launch(clsph_gpu* h) {
   (void)h;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   return 0;
 }
+
+namespace {
 
 // Two substeps captured once and replayed. The particle ids alternate between
 // their two buffers, so a pair returns them to the buffer it started from;
@@ -467,7 +292,7 @@ int sync_scene_tables(clsph_gpu* h) {
 
 extern "C" {
 
-const char* clsph_gpu_last_error(void) { return g_last_error.c_str(); }
+const char* clsph_gpu_last_error(void) { return clsph_host::g_last_error.c_str(); }
 
 int clsph_gpu_destroy(clsph_gpu* h);
 
@@ -577,6 +402,7 @@ int clsph_gpu_create(const clsph_parameters* params, const clsph_kernel_terms* t
 int clsph_gpu_destroy(clsph_gpu* h) {
   if (!h) return CLSPH_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->free_learned) h->free_learned(h);
   h->drop_graph();
   for (auto& t : h->pending) {
     cudaEventDestroy(t.start);

@@ -181,7 +181,7 @@ __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const
 // Grid set-up of every scene (sph_simulation.cpp:199-252), one thread per
 // scene, from the bounding boxes accumulated by the previous kernel; resets
 // the boxes, the radix digit totals and the sort control for this substep.
-__global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
+static __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
                              const float* __restrict__ scene_h, uint32_t nscenes,
                              uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
                              uint32_t* __restrict__ step_counters, uint32_t* __restrict__ ctl) {
@@ -233,7 +233,7 @@ __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restric
   }
 }
 
-__global__ void k_bbox_reset(uint32_t* __restrict__ bbox, uint32_t nscenes) {
+static __global__ void k_bbox_reset(uint32_t* __restrict__ bbox, uint32_t nscenes) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < 6 * nscenes; k += gridDim.x * blockDim.x)
     bbox[k] = (k % 6) < 3 ? f2ord(2147483648.0f) : f2ord(-2147483648.0f);
 }
@@ -301,7 +301,7 @@ __device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene,
 }
 
 // Host AoS (80-byte particle) -> SoA state, with bounding box.
-__global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State st,
+static __global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State st,
                              const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ bbox,
                              uint32_t* __restrict__ status) {
   const float qnan = __int_as_float(0x7FC00000);
@@ -329,7 +329,7 @@ __global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State s
 }
 
 // SoA -> host AoS: acceleration is 0 after the advection loop (sph.cl:97-99).
-__global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
+static __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
                            const float4* __restrict__ aux, const uint32_t* __restrict__ keys_base,
                            const uint32_t* __restrict__ ctl, int have_fields) {
   const KeySplit split{ctl[kCtlShift]};
@@ -352,7 +352,7 @@ __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
 }
 
 // Morton key per particle (grid.cl:56-66) and the largest key.
-__global__ void __launch_bounds__(kBlock)
+static __global__ void __launch_bounds__(kBlock)
     k_keys(const float4* __restrict__ pos, uint32_t n, const DevGrid* __restrict__ grids,
            const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
            uint32_t* __restrict__ keys) {
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(kBlock)
 // scatter per pass. Passes beyond DevGrid::passes return at once, so the
 // launch sequence is fixed (graph-capturable) while the work follows the
 // key width. Ping-pong: pass p reads buffer p&1 and writes (p+1)&1.
-__global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
+static __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
                               const uint32_t* __restrict__ ctl, uint32_t* __restrict__ tile_hist,
                               uint32_t ntiles, uint32_t* __restrict__ digit_total) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
@@ -406,7 +406,7 @@ __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n
 
 // One block per digit: exclusive scan of that digit's per-tile counts plus
 // the number of keys with a smaller digit.
-__global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, int pass,
+static __global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, int pass,
                              const uint32_t* __restrict__ ctl,
                              const uint32_t* __restrict__ digit_total) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
@@ -449,7 +449,7 @@ __global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, 
   }
 }
 
-__global__ void __launch_bounds__(kRadixThreads)
+static __global__ void __launch_bounds__(kRadixThreads)
     k_radix_scatter(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
                     int pass, const uint32_t* __restrict__ ctl,
                     const uint32_t* __restrict__ tile_hist, uint32_t ntiles) {
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kRadixThreads)
 // Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
 // and records every cell's [start, end) in the cell index (the dense cell
 // table of sph_simulation.cpp:162-170 in compact form).
-__global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
+static __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
                          const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
                          const uint32_t* __restrict__ keys_base,
                          const uint32_t* __restrict__ vals_base, State src, State dst,
@@ -737,18 +737,28 @@ __global__ void __launch_bounds__(BLOCK)
   ncount[i] = kept;  // > nlist_cap: the list is incomplete, forces search again
 }
 
+// Per-pair hook of k_forces (the learned stepper gathers its neighbour
+// features in the same walk); the plain substep uses this empty one.
+struct NoForceHook {
+  struct Acc {};
+  __device__ __forceinline__ Acc begin(uint32_t) const { return {}; }
+  __device__ __forceinline__ void pair(Acc&, uint32_t, uint32_t, const float4&, const float4&) const {}
+  __device__ __forceinline__ void end(Acc&, uint32_t, const float4&) const {}
+};
+
 // Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58), walking
 // the neighbour list of k_density (or the window, for overflowing lists).
-template <int BLOCK>
+template <int BLOCK, class Hook = NoForceHook>
 __global__ void __launch_bounds__(BLOCK)
     k_forces(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
              const uint32_t* __restrict__ ctl,
              const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,
              CellIndex ci, const Consts* __restrict__ consts, const uint32_t* __restrict__ nlist,
              const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
-             float4* __restrict__ acc_out) {
+             float4* __restrict__ acc_out, Hook hook) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  typename Hook::Acc ha = hook.begin(i);
   const uint32_t sc = scene_of[i];
   const Consts c = consts[sc];
   const float4 pi = st.pos[i];
@@ -763,6 +773,7 @@ __global__ void __launch_bounds__(BLOCK)
     const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
     const float rr = xnorm(d);
     force_pair(f, j == i, d, rr, vi, __ldg(&st.vel[j]), __ldg(&aux[j]), own, hh, lap_b, c);
+    hook.pair(ha, i, j, pi, pj);
   };
   const uint32_t cnt = ncount[i];
   if (cnt <= nlist_cap) {
@@ -779,7 +790,9 @@ __global__ void __launch_bounds__(BLOCK)
       if (xnorm(d) < c.h) pair(j);
     });
   }
-  acc_out[i] = finish_accel(f, ai.x, c);
+  const float4 a = finish_accel(f, ai.x, c);
+  acc_out[i] = a;
+  hook.end(ha, i, a);
 }
 
 // ------------------------------------------------------- mesh collision
@@ -856,11 +869,19 @@ __device__ __forceinline__ bool nearest_hit(const DevMesh& m, V3 p0, V3 p1, Hit&
 // Leapfrog + collision loop of sph.cl:64-112 (advection.cl:6-23,
 // collisions.cl:91-129), capped at max_iters passes; writes the new state
 // into `out` (same slots) and accumulates the next bounding box.
+// kLearned (the learned stepper, no counterpart in the reference): the step
+// spans dt_mult plain time steps, corr[i].xyz is added to the acceleration,
+// corr[i].w (the predicted density) is stored in out.vel.w, and positions
+// advance with (1 - pos_w) v + pos_w v' instead of v' (pos_w = (m + 1) / 2m
+// for m = dt_mult reproduces m leapfrog substeps exactly under constant
+// acceleration; m = 1 is the plain update).
+template <bool kLearned>
 __global__ void __launch_bounds__(kBlock)
     k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out,
              const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
              const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
-             uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count) {
+             uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count,
+             const float4* __restrict__ corr, float dt_mult, float pos_w) {
   const float qnan = __int_as_float(0x7FC00000);
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -876,6 +897,13 @@ __global__ void __launch_bounds__(kBlock)
     const V3 vh_old = v3(in.ivel[i]);
     V3 v = vh_old;
     V3 a = v3(acc[i]);
+    float predicted_rho = 0.f;
+    if constexpr (kLearned) {
+      remaining = XMUL(remaining, dt_mult);
+      const float4 d = corr[i];
+      a = {XADD(a.x, d.x), XADD(a.y, d.y), XADD(a.z, d.z)};
+      predicted_rho = d.w;
+    }
     bool capped = false;
     for (uint32_t it = 0;; ++it) {
       V3 nv = {XADD(v.x, XMUL(a.x, remaining)), XADD(v.y, XMUL(a.y, remaining)),
@@ -883,8 +911,14 @@ __global__ void __launch_bounds__(kBlock)
       const float sp = xnorm(nv);
       if (sp > c.vmax)
         nv = {XMUL(XDIV(nv.x, sp), c.vmax), XMUL(XDIV(nv.y, sp), c.vmax), XMUL(XDIV(nv.z, sp), c.vmax)};
-      const V3 np = {XADD(pos.x, XMUL(nv.x, remaining)), XADD(pos.y, XMUL(nv.y, remaining)),
-                     XADD(pos.z, XMUL(nv.z, remaining))};
+      V3 vp = nv;
+      if constexpr (kLearned) {
+        const float w0 = XSUB(1.f, pos_w);
+        vp = {XADD(XMUL(v.x, w0), XMUL(nv.x, pos_w)), XADD(XMUL(v.y, w0), XMUL(nv.y, pos_w)),
+              XADD(XMUL(v.z, w0), XMUL(nv.z, pos_w))};
+      }
+      const V3 np = {XADD(pos.x, XMUL(vp.x, remaining)), XADD(pos.y, XMUL(vp.y, remaining)),
+                     XADD(pos.z, XMUL(vp.z, remaining))};
       Hit h;
       const bool hit = nearest_hit(m, pos, np, h);
       float elapsed = remaining;
@@ -915,7 +949,7 @@ __global__ void __launch_bounds__(kBlock)
     out.pos[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
     out.ivel[i] = make_float4(v.x, v.y, v.z, 0.f);
     out.vel[i] = make_float4(XDIV(XADD(vh_old.x, v.x), 2.f), XDIV(XADD(vh_old.y, v.y), 2.f),
-                             XDIV(XADD(vh_old.z, v.z), 2.f), 0.f);
+                             XDIV(XADD(vh_old.z, v.z), 2.f), predicted_rho);
     if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
     lo = make_float3(pos.x, pos.y, pos.z);
     hi = lo;
@@ -926,7 +960,7 @@ __global__ void __launch_bounds__(kBlock)
 
 // Dense reference cell table of one scene from the sorted keys of its slot
 // range [first, last): table[c] = lower_bound(c) - first, c < cells.
-__global__ void k_dense_table(const uint32_t* __restrict__ keys_base, uint32_t n,
+static __global__ void k_dense_table(const uint32_t* __restrict__ keys_base, uint32_t n,
                               const uint32_t* __restrict__ ctl, const DevGrid* __restrict__ grid,
                               uint32_t scene, uint32_t first, uint32_t last,
                               uint32_t* __restrict__ table) {

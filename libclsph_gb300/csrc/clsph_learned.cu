@@ -1,0 +1,1092 @@
+// Learned 4x-dt stepper, sample collector and MLP training
+// (include/clsph_learned.h). No counterpart in the reference.
+//
+// The learned step reuses the plain substep's neighbour build, density and
+// force kernels on the handle's buffers, then runs
+//   k_forces<.., FeatureHook>  the plain forces kernel that also gathers 32
+//                   neighbour features per particle (sorted slot order),
+//                   standardised to BF16 rows
+//   k_mlp_infer     fused BF16 tensor-core MLP -> acceleration correction and
+//                   predicted density
+//   k_advect<true>  one leapfrog + collision pass over dt_mult time steps
+// and, at the next step, k_gate compares the density reached with the
+// prediction to accept the step or roll it back.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "clsph_handle.cuh"
+#include "clsph_learned.h"
+#include "clsph_mlp.cuh"
+#include "clsph_mlp_tc.cuh"
+
+using namespace clsph_host;
+using clsph_nn::bf16;
+using clsph_nn::kBlob;
+using clsph_nn::kHid;
+using clsph_nn::kIn;
+using clsph_nn::kOut;
+using clsph_nn::kOutPad;
+using clsph_nn::kParams;
+
+namespace {
+
+constexpr int kFeat = 32;
+static_assert(kFeat == kIn, "feature count");
+constexpr int kRing = 36;           // floats per tracked particle and level: features + naive v
+constexpr uint32_t kRowBlock = 2048;  // training rows come in multiples of this
+constexpr uint32_t kSplitK = 1024;    // batch rows per split of the weight-gradient GEMMs
+
+// ---------------------------------------------------------------------------
+// Features, gathered by k_forces in its neighbour walk (FeatureHook)
+
+enum FeatureMode { kFeatStd = 0, kFeatRaw = 1, kFeatRing = 2 };
+
+struct FeatureHook {
+  State st;  // sorted state of the current substep
+  const float4* aux;
+  const Consts* consts;
+  const uint16_t* scene_of;
+  int mode;
+  const float* norm;  // x_mu[32], x_sigma[32] (kFeatStd)
+  bf16* xstd;         // [n][32] (kFeatStd)
+  float* raw;         // [n][32] (kFeatRaw) or a ring level [m][kRing] (kFeatRing)
+  const uint32_t* ids;
+  uint32_t stride, m;
+
+  struct Acc {
+    float inv_h, vs, vx, vy, vz;
+    float s[22];  // sum w d (3), w d d^T (6), w u (3), w u u^T (6), w d.u, w d x u (3)
+    uint32_t cnt;
+  };
+
+  __device__ __forceinline__ Acc begin(uint32_t i) const {
+    Acc a;
+    const Consts& c = consts[scene_of[i]];
+    a.inv_h = 1.f / c.h;
+    a.vs = c.time_delta * c.scale * a.inv_h;
+    const float4 v = st.ivel[i];
+    a.vx = v.x;
+    a.vy = v.y;
+    a.vz = v.z;
+#pragma unroll
+    for (int k = 0; k < 22; ++k) a.s[k] = 0.f;
+    a.cnt = 0;
+    return a;
+  }
+
+  __device__ __forceinline__ void pair(Acc& a, uint32_t i, uint32_t j, const float4& pi, const float4& pj) const {
+    ++a.cnt;
+    if (j == i) return;
+    const float4 vj = __ldg(&st.ivel[j]);
+    const float dx = (pj.x - pi.x) * a.inv_h, dy = (pj.y - pi.y) * a.inv_h, dz = (pj.z - pi.z) * a.inv_h;
+    const float ux = (vj.x - a.vx) * a.vs, uy = (vj.y - a.vy) * a.vs, uz = (vj.z - a.vz) * a.vs;
+    const float w = fmaxf(0.f, 1.f - (dx * dx + dy * dy + dz * dz));
+    a.s[0] += w * dx;
+    a.s[1] += w * dy;
+    a.s[2] += w * dz;
+    a.s[3] += w * dx * dx;
+    a.s[4] += w * dy * dy;
+    a.s[5] += w * dz * dz;
+    a.s[6] += w * dx * dy;
+    a.s[7] += w * dx * dz;
+    a.s[8] += w * dy * dz;
+    a.s[9] += w * ux;
+    a.s[10] += w * uy;
+    a.s[11] += w * uz;
+    a.s[12] += w * ux * ux;
+    a.s[13] += w * uy * uy;
+    a.s[14] += w * uz * uz;
+    a.s[15] += w * ux * uy;
+    a.s[16] += w * ux * uz;
+    a.s[17] += w * uy * uz;
+    a.s[18] += w * (dx * ux + dy * uy + dz * uz);
+    a.s[19] += w * (dy * uz - dz * uy);
+    a.s[20] += w * (dz * ux - dx * uz);
+    a.s[21] += w * (dx * uy - dy * ux);
+  }
+
+  __device__ __forceinline__ void end(Acc& a, uint32_t i, const float4& acc) const {
+    uint32_t q = 0;
+    if (mode == kFeatRing) {
+      const uint32_t id = ids[i];
+      if (id % stride) return;
+      q = id / stride;
+      if (q >= m) return;
+    }
+    const Consts& c = consts[scene_of[i]];
+    const float4 ax = aux[i];
+    const float dt = c.time_delta * c.scale;
+    const float as = dt * dt * a.inv_h;
+    float f[kFeat];
+    f[0] = ax.x / c.rho0 - 1.f;
+    f[1] = c.K != 0.f ? ax.y / c.K : ax.y;
+    f[2] = (float)a.cnt * (1.f / 32.f);
+    f[3] = acc.x * as;
+    f[4] = acc.y * as;
+    f[5] = acc.z * as;
+    f[6] = a.vx * a.vs;
+    f[7] = a.vy * a.vs;
+    f[8] = a.vz * a.vs;
+    f[9] = c.vmax > 0.f ? sqrtf(a.vx * a.vx + a.vy * a.vy + a.vz * a.vz) / c.vmax : 0.f;
+#pragma unroll
+    for (int k = 0; k < 22; ++k) f[10 + k] = a.s[k];
+    if (mode == kFeatStd) {
+      uint4* row = reinterpret_cast<uint4*>(xstd + (size_t)i * kFeat);
+#pragma unroll
+      for (int qq = 0; qq < kFeat / 8; ++qq) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int k = qq * 8 + 2 * e;
+          w[e] = clsph_nn::pack_bf16((f[k] - norm[k]) / norm[kFeat + k],
+                                      (f[k + 1] - norm[k + 1]) / norm[kFeat + k + 1]);
+        }
+        row[qq] = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    } else {
+      float* out = mode == kFeatRaw ? raw + (size_t)i * kFeat : raw + (size_t)q * kRing;
+#pragma unroll
+      for (int k = 0; k < kFeat; ++k) out[k] = f[k];
+    }
+  }
+};
+
+// the naive dt_mult step's velocity (units h/dt) of the tracked particles
+__global__ void __launch_bounds__(kBlock)
+    k_ring_naive(uint32_t n, const uint32_t* __restrict__ ids, uint32_t stride, uint32_t m,
+                 const float4* __restrict__ naive_ivel, const Consts* __restrict__ consts,
+                 const uint16_t* __restrict__ scene_of, float* __restrict__ level) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t id = ids[i];
+  if (id % stride) return;
+  const uint32_t q = id / stride;
+  if (q >= m) return;
+  const Consts& c = consts[scene_of[i]];
+  const float vs = c.time_delta * c.scale / c.h;
+  const float4 v = naive_ivel[i];
+  float* out = level + (size_t)q * kRing;
+  out[32] = v.x * vs;
+  out[33] = v.y * vs;
+  out[34] = v.z * vs;
+  out[35] = 0.f;
+}
+
+// samples from two ring levels dt_mult substeps apart
+__global__ void k_sample(const float* __restrict__ old_level, const float* __restrict__ now_level,
+                         uint32_t m, float inv_mult, float* __restrict__ xs, float* __restrict__ ys,
+                         uint64_t base, uint64_t capacity) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const uint64_t s = base + q;
+  if (s >= capacity) return;
+  const float* o = old_level + (size_t)q * kRing;
+  const float* w = now_level + (size_t)q * kRing;
+  for (int k = 0; k < kFeat; ++k) xs[s * kFeat + k] = o[k];
+  ys[s * kOut + 0] = (w[6] - o[32]) * inv_mult;
+  ys[s * kOut + 1] = (w[7] - o[33]) * inv_mult;
+  ys[s * kOut + 2] = (w[8] - o[34]) * inv_mult;
+  ys[s * kOut + 3] = (w[0] + 1.f) / (o[0] + 1.f) - 1.f;
+}
+
+// sum over particles of |rho - rho_predicted| / rho0 (predicted density in vel.w)
+__global__ void __launch_bounds__(kBlock)
+    k_gate(uint32_t n, const float4* __restrict__ aux, const float4* __restrict__ vel,
+           const Consts* __restrict__ consts, const uint16_t* __restrict__ scene_of,
+           float* __restrict__ dev_sum) {
+  __shared__ float red[kBlock / 32];
+  float s = 0.f;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s += fabsf(aux[i].x - vel[i].w) / consts[scene_of[i]].rho0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < kBlock / 32; ++w) t += red[w];
+    atomicAdd(dev_sum, t);
+  }
+}
+
+// MLP outputs -> physical acceleration correction and predicted density
+struct StoreCorr {
+  float4* corr;
+  const float4* aux;
+  const Consts* consts;
+  const uint16_t* scene_of;
+  __device__ void operator()(uint32_t row, float4 y) const {
+    const Consts& c = consts[scene_of[row]];
+    const float dt = c.time_delta * c.scale;
+    const float s = c.h / (dt * dt);
+    corr[row] = make_float4(y.x * s, y.y * s, y.z * s, aux[row].x * (1.f + y.w));
+  }
+};
+
+template <class Store>
+int launch_infer(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows,
+                 const clsph_nn::InferWeights& w, Store store, clsph_gpu* h, int cls) {
+  // set on every launch: the attribute belongs to the current device
+  cudaError_t e = cudaFuncSetAttribute(clsph_nn::k_mlp_infer<Store>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)clsph_nn::kInferSmem);
+  if (e != cudaSuccess)
+    return fail(CLSPH_ERR_CUDA, std::string("mlp: shared memory attribute: ") + cudaGetErrorString(e));
+  const uint32_t tiles = (rows + 15) / 16;
+  uint32_t blocks = (tiles + clsph_nn::kInferWarps - 1) / clsph_nn::kInferWarps;
+  blocks = std::max(1u, std::min(blocks, sms));
+  if (h)
+    h->launch_smem(cls, clsph_nn::k_mlp_infer<Store>, dim3(blocks), dim3(clsph_nn::kInferWarps * 32),
+                   clsph_nn::kInferSmem, x, rows, w, store);
+  else
+    clsph_nn::k_mlp_infer<Store><<<blocks, clsph_nn::kInferWarps * 32, clsph_nn::kInferSmem, stream>>>(
+        x, rows, w, store);
+  return 0;
+}
+
+// tcgen05 inference; *err collects wait timeouts (see k_mlp_tc)
+template <class Store>
+int launch_tc(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows, const clsph_nn::TcWeights& w,
+              Store store, uint32_t* err, clsph_gpu* h, int cls) {
+  cudaError_t e = cudaFuncSetAttribute(clsph_nn::k_mlp_tc<Store>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)clsph_nn::kTcSmem);
+  if (e != cudaSuccess)
+    return fail(CLSPH_ERR_CUDA, std::string("mlp: shared memory attribute: ") + cudaGetErrorString(e));
+  const uint32_t tiles = (rows + clsph_nn::kTcRows - 1) / clsph_nn::kTcRows;
+  const uint32_t blocks = std::max(1u, std::min(tiles, sms));
+  if (h)
+    h->launch_smem(cls, clsph_nn::k_mlp_tc<Store>, dim3(blocks), dim3(clsph_nn::kTcThreads), clsph_nn::kTcSmem,
+                   x, rows, w, store, err);
+  else
+    clsph_nn::k_mlp_tc<Store><<<blocks, clsph_nn::kTcThreads, clsph_nn::kTcSmem, stream>>>(x, rows, w, store, err);
+  return 0;
+}
+
+// weight of the end-of-step velocity in the position update of one step over
+// m time steps: sum_{k=1..m} v_k dt = m dt ((1 - w) v_0 + w v_m), w = (m + 1) / 2m,
+// for constant acceleration
+float position_weight(uint32_t m) { return (float)(m + 1) / (float)(2 * m); }
+
+FeatureHook feature_hook(clsph_gpu* h, int mode) {
+  FeatureHook f{};
+  f.st = h->st[1];
+  f.aux = h->aux;
+  f.consts = h->consts;
+  f.scene_of = h->scene_of;
+  f.mode = mode;
+  f.stride = 1;
+  return f;
+}
+
+// the forces kernel of the current substep again (same accelerations), with
+// the feature gathering
+int launch_forces_hooked(clsph_gpu* h, const FeatureHook& hook) {
+  const int b = h->forces_block;
+  const dim3 grid((h->n + b - 1) / b);
+  auto go = [&](auto kernel) {
+    h->launch(K_FEATURES, kernel, grid, dim3(b), h->n, (const DevGrid*)h->grids,
+              (const uint16_t*)h->scene_of, (const uint32_t*)h->ctl, (const uint32_t*)h->keys, h->st[1],
+              (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
+              (const uint32_t*)h->ncount, h->nlist_cap, h->acc, hook);
+  };
+  if (b == 64) go(k_forces<64, FeatureHook>);
+  else if (b == 256) go(k_forces<256, FeatureHook>);
+  else go(k_forces<128, FeatureHook>);
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// MLP handle
+
+struct clsph_mlp {
+  int device = 0;
+  uint32_t sms = 152;
+  cudaStream_t stream = nullptr;
+  float* blob = nullptr;  // kBlob floats
+  bf16* w1b = nullptr;    // [32][256]
+  bf16* w2b = nullptr;    // [256][256]
+  bf16* w3b = nullptr;    // [256][8]
+  bf16* w1t = nullptr;    // [256][32]
+  bf16* w2t = nullptr;    // [256][256]
+  uint32_t* err = nullptr;  // tensor-core wait timeouts of clsph_mlp_forward
+  // training state, made on first use
+  uint32_t rows_cap = 0;
+  float* grad = nullptr;
+  float* adam_m = nullptr;
+  float* adam_v = nullptr;
+  uint64_t adam_t = 0;
+  bf16 *xb = nullptr, *h1 = nullptr, *h2 = nullptr, *dz1 = nullptr, *dz2 = nullptr;
+  float *yb = nullptr, *z1 = nullptr, *z2 = nullptr, *ws = nullptr, *loss = nullptr;
+  uint32_t loss_cap = 0;
+  uint32_t* idx = nullptr;
+  uint64_t idx_cap = 0;
+  double* moments = nullptr;
+
+};
+
+namespace {
+
+clsph_nn::Bf16Weights bf16_weights(const clsph_mlp* m) {
+  return clsph_nn::Bf16Weights{m->w1b, m->w2b, m->w3b, m->w1t, m->w2t};
+}
+
+clsph_nn::TcWeights tc_weights(const clsph_mlp* m) {
+  return clsph_nn::TcWeights{m->w1t,
+                             m->w2t,
+                             m->blob + clsph_nn::kOffW3,
+                             m->blob + clsph_nn::kOffB1,
+                             m->blob + clsph_nn::kOffB2,
+                             m->blob + clsph_nn::kOffB3,
+                             m->blob + clsph_nn::kOffYMu,
+                             m->blob + clsph_nn::kOffYSigma};
+}
+
+clsph_nn::InferWeights infer_weights(const clsph_mlp* m) {
+  return clsph_nn::InferWeights{m->w1b,
+                                 m->w2b,
+                                 m->w3b,
+                                 m->blob + clsph_nn::kOffB1,
+                                 m->blob + clsph_nn::kOffB2,
+                                 m->blob + clsph_nn::kOffB3,
+                                 m->blob + clsph_nn::kOffYMu,
+                                 m->blob + clsph_nn::kOffYSigma};
+}
+
+}  // namespace
+
+namespace {
+
+using clsph_nn::EpiGeluGrad;
+using clsph_nn::EpiHidden;
+using clsph_nn::EpiPartial;
+using clsph_nn::GemmSmem;
+
+template <int WM, int WN, bool A_K, bool B_K, class Epi>
+int gemm(cudaStream_t s, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int k_split,
+         Epi epi) {
+  using S = GemmSmem<WM, WN, A_K, B_K>;
+  if (M % S::BM || N % S::BN || K % k_split || k_split % clsph_nn::kGemmBK || lda % 8 || ldb % 8)
+    return fail(CLSPH_ERR_ARGUMENT, "mlp: GEMM shape not tileable");
+  dim3 grid(N / S::BN, M / S::BM, K / k_split);
+  clsph_nn::k_gemm<WM, WN, A_K, B_K, Epi><<<grid, 128, S::BYTES, s>>>(A, lda, B, ldb, M, N, K, k_split, epi);
+  return 0;
+}
+
+template <class T>
+int alloc(T** p, size_t count) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("mlp: cudaMalloc: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int ensure_training(clsph_mlp* m, uint32_t rows) {
+  if (!m->grad) {
+    int rc;
+    if ((rc = alloc(&m->grad, kParams)) || (rc = alloc(&m->adam_m, kParams)) ||
+        (rc = alloc(&m->adam_v, kParams)) || (rc = alloc(&m->moments, 2 * (kIn + kOut))))
+      return rc;
+    CUDA_TRY(cudaMemset(m->adam_m, 0, sizeof(float) * kParams));
+    CUDA_TRY(cudaMemset(m->adam_v, 0, sizeof(float) * kParams));
+    m->adam_t = 0;
+  }
+  if (rows > m->rows_cap) {
+    void* bufs[] = {m->xb, m->h1, m->h2, m->dz1, m->dz2, m->yb, m->z1, m->z2, m->ws};
+    for (void* b : bufs) cudaFree(b);
+    const size_t r = rows;
+    int rc;
+    if ((rc = alloc(&m->xb, r * kIn)) || (rc = alloc(&m->h1, r * kHid)) || (rc = alloc(&m->h2, r * kHid)) ||
+        (rc = alloc(&m->dz1, r * kHid)) || (rc = alloc(&m->dz2, r * kHid)) || (rc = alloc(&m->yb, r * kOut)) ||
+        (rc = alloc(&m->z1, r * kHid)) || (rc = alloc(&m->z2, r * kHid)) ||
+        (rc = alloc(&m->ws, (r / kSplitK) * (size_t)kHid * kHid)))
+      return rc;
+    m->rows_cap = rows;
+  }
+  return 0;
+}
+
+int ensure_idx(clsph_mlp* m, uint64_t count) {
+  if (count > m->idx_cap) {
+    cudaFree(m->idx);
+    m->idx = nullptr;
+    int rc = alloc(&m->idx, count);
+    if (rc) return rc;
+    m->idx_cap = count;
+  }
+  return 0;
+}
+
+int ensure_loss(clsph_mlp* m, uint32_t count) {
+  if (count > m->loss_cap) {
+    cudaFree(m->loss);
+    m->loss = nullptr;
+    int rc = alloc(&m->loss, count);
+    if (rc) return rc;
+    m->loss_cap = count;
+  }
+  return 0;
+}
+
+// Forward + loss (into *loss_slot) and, when `backward`, gradients into
+// m->grad for the `rows` rows already in m->xb / m->yb.
+int pass(clsph_mlp* m, uint32_t rows, float* loss_slot, bool backward) {
+  cudaStream_t s = m->stream;
+  const float* p = m->blob;
+  int rc;
+  if (backward) CUDA_TRY(cudaMemsetAsync(m->grad, 0, sizeof(float) * kParams, s));
+  // Z1 = X W1 + b1, H1 = GELU(Z1)
+  if ((rc = gemm<2, 2, true, false>(s, m->xb, kIn, m->w1b, kHid, rows, kHid, kIn, kIn,
+                                    EpiHidden{p + clsph_nn::kOffB1, m->z1, m->h1, kHid})))
+    return rc;
+  // Z2 = H1 W2 + b2, H2 = GELU(Z2)
+  if ((rc = gemm<2, 2, true, false>(s, m->h1, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
+                                    EpiHidden{p + clsph_nn::kOffB2, m->z2, m->h2, kHid})))
+    return rc;
+  // Y = H2 W3 + b3, loss, dZ2, dW3, db3
+  clsph_nn::k_head<<<rows / 256, kHid, 0, s>>>(m->h2, m->z2, p + clsph_nn::kOffW3, p + clsph_nn::kOffB3, m->yb,
+                                               rows, 256, 1.f / rows, m->dz2, m->grad + clsph_nn::kOffW3,
+                                               m->grad + clsph_nn::kOffB3, loss_slot, nullptr);
+  if (!backward) return 0;
+  const int splits = rows / kSplitK;
+  const size_t split_stride = (size_t)kHid * kHid;
+  // dW2 = H1^T dZ2 (split over rows), db2 = column sums of dZ2
+  if ((rc = gemm<2, 2, false, false>(s, m->h1, kHid, m->dz2, kHid, kHid, kHid, rows, kSplitK,
+                                     EpiPartial{m->ws, kHid, split_stride})))
+    return rc;
+  clsph_nn::k_reduce_splits<<<(kHid * kHid + 255) / 256, 256, 0, s>>>(m->ws, splits, (size_t)kHid * kHid,
+                                                                      m->grad + clsph_nn::kOffW2);
+  clsph_nn::k_colsum<<<rows / 256, kHid, 0, s>>>(m->dz2, rows, kHid, 256, m->grad + clsph_nn::kOffB2);
+  // dZ1 = (dZ2 W2^T) * GELU'(Z1)
+  if ((rc = gemm<2, 2, true, true>(s, m->dz2, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
+                                   EpiGeluGrad{m->z1, m->dz1, kHid})))
+    return rc;
+  // dW1 = X^T dZ1, db1
+  if ((rc = gemm<1, 4, false, false>(s, m->xb, kIn, m->dz1, kHid, kIn, kHid, rows, kSplitK,
+                                     EpiPartial{m->ws, kHid, (size_t)kIn * kHid})))
+    return rc;
+  clsph_nn::k_reduce_splits<<<(kIn * kHid + 255) / 256, 256, 0, s>>>(m->ws, splits, (size_t)kIn * kHid,
+                                                                    m->grad + clsph_nn::kOffW1);
+  clsph_nn::k_colsum<<<rows / 256, kHid, 0, s>>>(m->dz1, rows, kHid, 256, m->grad + clsph_nn::kOffB1);
+  return 0;
+}
+
+int refresh_bf16(clsph_mlp* m) {
+  clsph_nn::k_refresh_bf16<<<(kParams + 255) / 256, 256, 0, m->stream>>>(m->blob, bf16_weights(m));
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// Learned-step buffers of one engine handle.
+struct Snapshot {
+  float4 *pos = nullptr, *vel = nullptr, *ivel = nullptr;
+  uint32_t* ids = nullptr;
+  uint32_t* bbox = nullptr;
+  int ids_sel = 0;
+};
+
+struct LearnedCache {
+  bf16* x = nullptr;       // [n][32]
+  float4* corr = nullptr;  // [n]
+  Snapshot snap[2];
+  float* dev_sum = nullptr;   // [0] deviation sum, [1] tensor-core error word
+  float* dev_host = nullptr;  // pinned copy of both
+  cudaEvent_t ev = nullptr;
+};
+
+void free_cache(clsph_gpu* h) {
+  auto* L = static_cast<LearnedCache*>(h->learned);
+  if (!L) return;
+  cudaFree(L->x);
+  cudaFree(L->corr);
+  for (auto& s : L->snap) {
+    cudaFree(s.pos);
+    cudaFree(s.vel);
+    cudaFree(s.ivel);
+    cudaFree(s.ids);
+    cudaFree(s.bbox);
+  }
+  cudaFree(L->dev_sum);
+  if (L->dev_host) cudaFreeHost(L->dev_host);
+  if (L->ev) cudaEventDestroy(L->ev);
+  delete L;
+  h->learned = nullptr;
+}
+
+int ensure_cache(clsph_gpu* h, LearnedCache** out) {
+  if (h->learned) {
+    *out = static_cast<LearnedCache*>(h->learned);
+    return 0;
+  }
+  auto* L = new LearnedCache();
+  h->learned = L;
+  h->free_learned = free_cache;
+  const size_t n = h->n;
+  int rc;
+  if ((rc = dev_alloc(&L->x, n * kFeat)) || (rc = dev_alloc(&L->corr, n)) || (rc = dev_alloc(&L->dev_sum, 2)))
+    return rc;
+  CUDA_TRY(cudaMemset(L->dev_sum, 0, 2 * sizeof(float)));
+  for (auto& s : L->snap)
+    if ((rc = dev_alloc(&s.pos, n)) || (rc = dev_alloc(&s.vel, n)) || (rc = dev_alloc(&s.ivel, n)) ||
+        (rc = dev_alloc(&s.ids, n)) || (rc = dev_alloc(&s.bbox, 6 * (size_t)h->nscenes)))
+      return rc;
+  CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), 2 * sizeof(float)));
+  CUDA_TRY(cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming));
+  *out = L;
+  return 0;
+}
+
+int save(clsph_gpu* h, Snapshot& s) {
+  const size_t b = sizeof(float4) * h->n;
+  CUDA_TRY(cudaMemcpyAsync(s.pos, h->st[0].pos, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(s.vel, h->st[0].vel, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(s.ivel, h->st[0].ivel, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(s.ids, h->ids[h->ids_sel], sizeof(uint32_t) * h->n, cudaMemcpyDeviceToDevice,
+                           h->stream));
+  CUDA_TRY(cudaMemcpyAsync(s.bbox, h->bbox, sizeof(uint32_t) * 6 * h->nscenes, cudaMemcpyDeviceToDevice,
+                           h->stream));
+  s.ids_sel = h->ids_sel;
+  return 0;
+}
+
+int restore(clsph_gpu* h, const Snapshot& s) {
+  const size_t b = sizeof(float4) * h->n;
+  CUDA_TRY(cudaMemcpyAsync(h->st[0].pos, s.pos, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->st[0].vel, s.vel, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->st[0].ivel, s.ivel, b, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->ids[s.ids_sel], s.ids, sizeof(uint32_t) * h->n, cudaMemcpyDeviceToDevice,
+                           h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->bbox, s.bbox, sizeof(uint32_t) * 6 * h->nscenes, cudaMemcpyDeviceToDevice,
+                           h->stream));
+  h->ids_sel = s.ids_sel;
+  return 0;
+}
+
+// density check of the state just sorted and evaluated: mean |rho - rho_pred| / rho0
+int enqueue_gate(clsph_gpu* h, LearnedCache* L) {
+  CUDA_TRY(cudaMemsetAsync(L->dev_sum, 0, sizeof(float), h->stream));
+  h->launch(K_GATE, k_gate, dim3(grid_blocks(h->n, h->sm_count * 4)), dim3(kBlock), h->n,
+            (const float4*)h->aux, (const float4*)h->st[1].vel, (const Consts*)h->consts,
+            (const uint16_t*)h->scene_of, L->dev_sum);
+  CUDA_TRY(cudaMemcpyAsync(L->dev_host, L->dev_sum, 2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaEventRecord(L->ev, h->stream));
+  return 0;
+}
+
+int wait_gate(clsph_gpu* h, LearnedCache* L, double* dev) {
+  CUDA_TRY(cudaEventSynchronize(L->ev));
+  uint32_t errw;
+  std::memcpy(&errw, L->dev_host + 1, sizeof(errw));
+  if (errw) return fail(CLSPH_ERR_CUDA, "step_learned: a tensor-core wait of the MLP kernel timed out");
+  *dev = (double)L->dev_host[0] / (double)h->n;
+  return 0;
+}
+
+// forces + features -> MLP -> one advection over dt_mult time steps
+int enqueue_learned_tail(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t dt_mult) {
+  const uint32_t n = h->n;
+  FeatureHook fh = feature_hook(h, kFeatStd);
+  fh.norm = m->blob + clsph_nn::kOffXMu;
+  fh.xstd = L->x;
+  int rc = launch_forces_hooked(h, fh);
+  if (rc) return rc;
+  rc = launch_tc(h->stream, h->sm_count, L->x, n, tc_weights(m),
+                     StoreCorr{L->corr, h->aux, h->consts, h->scene_of},
+                     reinterpret_cast<uint32_t*>(L->dev_sum + 1), h, K_MLP);
+  if (rc) return rc;
+  h->launch(K_LEARNED_ADVECT, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
+            dim3(kBlock), n, h->st[1], (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes,
+            (const Consts*)h->consts, (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status,
+            h->capped, (const float4*)L->corr, (float)dt_mult, position_weight(dt_mult));
+  return 0;
+}
+
+int plain_substeps(clsph_gpu* h, uint32_t count) {
+  for (uint32_t k = 0; k < count; ++k) {
+    int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+    if (rc) return rc;
+    ++h->substeps;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Collector
+
+struct clsph_collector {
+  clsph_gpu* h = nullptr;
+  uint32_t stride = 1, m = 0, dt_mult = 4;
+  uint64_t capacity = 0, count = 0, t = 0;
+  float* ring = nullptr;  // (dt_mult + 1) levels x m x kRing
+  float* xs = nullptr;
+  float* ys = nullptr;
+  State scratch{};
+  float4* zero = nullptr;
+  uint32_t* sbbox = nullptr;
+  uint32_t* sstatus = nullptr;
+  unsigned long long* scapped = nullptr;
+};
+
+extern "C" {
+
+uint64_t clsph_mlp_blob_size(void) { return kBlob; }
+
+int clsph_mlp_destroy(clsph_mlp* m) {
+  if (!m) return CLSPH_OK;
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  void* bufs[] = {m->blob, m->w1b, m->w2b, m->w3b, m->w1t,  m->w2t,    m->err,    m->grad,
+                  m->adam_m, m->adam_v, m->xb, m->h1, m->h2, m->dz1, m->dz2, m->yb, m->z1, m->z2,
+                  m->ws,   m->loss, m->idx, m->moments};
+  for (void* b : bufs) cudaFree(b);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return CLSPH_OK;
+}
+
+int clsph_mlp_create(uint64_t seed, clsph_mlp** out) {
+  if (!out) return fail(CLSPH_ERR_ARGUMENT, "mlp_create: null output");
+  int devices = 0;
+  if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
+    return fail(CLSPH_ERR_NO_DEVICE, "mlp_create: no CUDA device");
+  auto* m = new clsph_mlp();
+  cudaGetDevice(&m->device);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device) == cudaSuccess && sms > 0)
+    m->sms = (uint32_t)sms;
+  auto bail = [&](int rc) {
+    clsph_mlp_destroy(m);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "mlp_create: stream"));
+  int rc;
+  if ((rc = alloc(&m->blob, kBlob)) || (rc = alloc(&m->w1b, kIn * kHid)) || (rc = alloc(&m->w2b, kHid * kHid)) ||
+      (rc = alloc(&m->w3b, kHid * kOutPad)) || (rc = alloc(&m->w1t, kIn * kHid)) ||
+      (rc = alloc(&m->w2t, kHid * kHid)) || (rc = alloc(&m->err, 1)))
+    return bail(rc);
+  if (cudaMemset(m->err, 0, sizeof(uint32_t)) != cudaSuccess) return bail(fail(CLSPH_ERR_CUDA, "mlp_create: memset"));
+  std::vector<float> blob(kBlob, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  const float s1 = std::sqrt(2.f / kIn), s2 = std::sqrt(2.f / kHid), s3 = 0.01f * std::sqrt(1.f / kHid);
+  for (int i = 0; i < kIn * kHid; ++i) blob[clsph_nn::kOffW1 + i] = nd(rng) * s1;
+  for (int i = 0; i < kHid * kHid; ++i) blob[clsph_nn::kOffW2 + i] = nd(rng) * s2;
+  for (int i = 0; i < kHid * kOut; ++i) blob[clsph_nn::kOffW3 + i] = nd(rng) * s3;
+  for (int i = 0; i < kIn; ++i) blob[clsph_nn::kOffXSigma + i] = 1.f;
+  for (int i = 0; i < kOut; ++i) blob[clsph_nn::kOffYSigma + i] = 1.f;
+  if (cudaMemcpy(m->blob, blob.data(), sizeof(float) * kBlob, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "mlp_create: upload"));
+  if ((rc = refresh_bf16(m)) || cudaStreamSynchronize(m->stream) != cudaSuccess)
+    return bail(rc ? rc : fail(CLSPH_ERR_CUDA, "mlp_create: weight conversion"));
+  *out = m;
+  return CLSPH_OK;
+}
+
+int clsph_mlp_set_blob(clsph_mlp* m, const float* blob, uint64_t count) {
+  if (!m || !blob || count != kBlob) return fail(CLSPH_ERR_ARGUMENT, "mlp_set_blob: bad argument");
+  for (int i = 0; i < kIn; ++i)
+    if (!(blob[clsph_nn::kOffXSigma + i] > 0.f)) return fail(CLSPH_ERR_ARGUMENT, "mlp_set_blob: x_sigma <= 0");
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  CUDA_TRY(cudaMemcpy(m->blob, blob, sizeof(float) * kBlob, cudaMemcpyHostToDevice));
+  int rc = refresh_bf16(m);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  m->adam_t = 0;
+  if (m->adam_m) {
+    CUDA_TRY(cudaMemset(m->adam_m, 0, sizeof(float) * kParams));
+    CUDA_TRY(cudaMemset(m->adam_v, 0, sizeof(float) * kParams));
+  }
+  return CLSPH_OK;
+}
+
+int clsph_mlp_get_blob(clsph_mlp* m, float* blob, uint64_t count) {
+  if (!m || !blob || count != kBlob) return fail(CLSPH_ERR_ARGUMENT, "mlp_get_blob: bad argument");
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  CUDA_TRY(cudaMemcpy(blob, m->blob, sizeof(float) * kBlob, cudaMemcpyDeviceToHost));
+  return CLSPH_OK;
+}
+
+int clsph_mlp_forward(clsph_mlp* m, const uint16_t* x_bf16, uint32_t rows, float* y, void* cuda_stream) {
+  if (!m || (rows && (!x_bf16 || !y))) return fail(CLSPH_ERR_ARGUMENT, "mlp_forward: bad argument");
+  if (!rows) return CLSPH_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  int rc = launch_tc(s, m->sms, reinterpret_cast<const bf16*>(x_bf16), rows, tc_weights(m),
+                     clsph_nn::StoreRaw{reinterpret_cast<float4*>(y)}, m->err, nullptr, 0);
+  if (rc) return rc;
+  CUDA_TRY(cudaGetLastError());
+  return CLSPH_OK;
+}
+
+int clsph_mlp_forward_mma_sync(clsph_mlp* m, const uint16_t* x_bf16, uint32_t rows, float* y, void* cuda_stream) {
+  if (!m || (rows && (!x_bf16 || !y))) return fail(CLSPH_ERR_ARGUMENT, "mlp_forward_mma_sync: bad argument");
+  if (!rows) return CLSPH_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  int rc = launch_infer(s, m->sms, reinterpret_cast<const bf16*>(x_bf16), rows, infer_weights(m),
+                        clsph_nn::StoreRaw{reinterpret_cast<float4*>(y)}, nullptr, 0);
+  if (rc) return rc;
+  CUDA_TRY(cudaGetLastError());
+  return CLSPH_OK;
+}
+
+int clsph_mlp_predict(clsph_mlp* m, const float* x_raw, uint64_t rows, float* y_host) {
+  if (!m || (rows && (!x_raw || !y_host))) return fail(CLSPH_ERR_ARGUMENT, "mlp_predict: bad argument");
+  const uint32_t chunk = 65536;
+  int rc;
+  if ((rc = ensure_training(m, chunk))) return rc;
+  for (uint64_t off = 0; off < rows; off += chunk) {
+    const uint32_t r = (uint32_t)std::min<uint64_t>(chunk, rows - off);
+    clsph_nn::k_standardize<<<(r * kIn + 255) / 256, 256, 0, m->stream>>>(x_raw + off * kIn, r,
+                                                                        m->blob + clsph_nn::kOffXMu, m->xb);
+    if ((rc = launch_tc(m->stream, m->sms, m->xb, r, tc_weights(m), clsph_nn::StoreRaw{reinterpret_cast<float4*>(m->yb)},
+                        m->err, nullptr, 0)))
+      return rc;
+    CUDA_TRY(cudaMemcpyAsync(y_host + off * kOut, m->yb, sizeof(float) * kOut * r, cudaMemcpyDeviceToHost,
+                             m->stream));
+    CUDA_TRY(cudaStreamSynchronize(m->stream));
+  }
+  uint32_t e = 0;
+  CUDA_TRY(cudaMemcpy(&e, m->err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e) return fail(CLSPH_ERR_CUDA, "mlp_predict: a tensor-core wait timed out");
+  return CLSPH_OK;
+}
+
+int clsph_mlp_status(clsph_mlp* m, uint32_t* flags) {
+  if (!m || !flags) return fail(CLSPH_ERR_ARGUMENT, "mlp_status: bad argument");
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(flags, m->err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemset(m->err, 0, sizeof(uint32_t)));
+  return CLSPH_OK;
+}
+
+int clsph_mlp_gradients(clsph_mlp* m, const float* x_raw, const float* y_raw, uint32_t rows,
+                        float* grads_host, float* loss) {
+  if (!m || !x_raw || !y_raw || rows == 0 || rows % kRowBlock)
+    return fail(CLSPH_ERR_ARGUMENT, "mlp_gradients: rows must be a positive multiple of 2048");
+  int rc;
+  if ((rc = ensure_training(m, rows)) || (rc = ensure_idx(m, rows)) || (rc = ensure_loss(m, 1))) return rc;
+  std::vector<uint32_t> iota(rows);
+  std::iota(iota.begin(), iota.end(), 0u);
+  CUDA_TRY(cudaMemcpyAsync(m->idx, iota.data(), sizeof(uint32_t) * rows, cudaMemcpyHostToDevice, m->stream));
+  CUDA_TRY(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
+  clsph_nn::k_gather_batch<<<(rows * (kIn + kOut) + 255) / 256, 256, 0, m->stream>>>(
+      x_raw, y_raw, m->idx, rows, m->blob + clsph_nn::kOffXMu, m->xb, m->yb);
+  if ((rc = pass(m, rows, m->loss, true))) return rc;
+  float l = 0.f;
+  CUDA_TRY(cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+  if (grads_host)
+    CUDA_TRY(cudaMemcpyAsync(grads_host, m->grad, sizeof(float) * kParams, cudaMemcpyDeviceToHost, m->stream));
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  if (loss) *loss = l / rows;
+  return CLSPH_OK;
+}
+
+int clsph_mlp_loss(clsph_mlp* m, const float* x_raw, const float* y_raw, uint64_t samples, float* loss) {
+  if (!m || !x_raw || !y_raw || !loss) return fail(CLSPH_ERR_ARGUMENT, "mlp_loss: bad argument");
+  const uint32_t rows = (uint32_t)std::min<uint64_t>(samples - samples % kRowBlock, 65536);
+  if (rows == 0) return fail(CLSPH_ERR_ARGUMENT, "mlp_loss: fewer than 2048 samples");
+  const uint64_t blocks = samples / rows;
+  int rc;
+  if ((rc = ensure_training(m, rows)) || (rc = ensure_idx(m, rows)) || (rc = ensure_loss(m, 1))) return rc;
+  CUDA_TRY(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
+  std::vector<uint32_t> iota(rows);
+  for (uint64_t b = 0; b < blocks; ++b) {
+    for (uint32_t r = 0; r < rows; ++r) iota[r] = (uint32_t)(b * rows + r);
+    CUDA_TRY(cudaMemcpyAsync(m->idx, iota.data(), sizeof(uint32_t) * rows, cudaMemcpyHostToDevice, m->stream));
+    clsph_nn::k_gather_batch<<<(rows * (kIn + kOut) + 255) / 256, 256, 0, m->stream>>>(
+        x_raw, y_raw, m->idx, rows, m->blob + clsph_nn::kOffXMu, m->xb, m->yb);
+    if ((rc = pass(m, rows, m->loss, false))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(m->stream));  // iota is reused
+  }
+  float l = 0.f;
+  CUDA_TRY(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
+  *loss = l / (float)(blocks * rows);
+  return CLSPH_OK;
+}
+
+int clsph_mlp_train(clsph_mlp* m, const float* x_raw, const float* y_raw, uint64_t samples,
+                    const clsph_train_config* cfg, float* loss_log, uint32_t log_len, uint32_t* logged) {
+  if (!m || !x_raw || !y_raw || !cfg || cfg->batch == 0 || cfg->batch % kRowBlock || cfg->epochs == 0)
+    return fail(CLSPH_ERR_ARGUMENT, "mlp_train: bad argument (batch must be a multiple of 2048)");
+  if (samples < cfg->batch || samples >= (1ull << 32))
+    return fail(CLSPH_ERR_ARGUMENT, "mlp_train: sample count out of range");
+  const uint32_t rows = cfg->batch;
+  int rc;
+  if ((rc = ensure_training(m, rows)) || (rc = ensure_idx(m, samples))) return rc;
+  cudaStream_t s = m->stream;
+  if (cfg->fit_normalisation) {
+    CUDA_TRY(cudaMemsetAsync(m->moments, 0, sizeof(double) * 2 * (kIn + kOut), s));
+    const uint64_t per = 4096;
+    clsph_nn::k_moments<<<(unsigned)((samples + per - 1) / per), 64, 0, s>>>(x_raw, y_raw, samples, per,
+                                                                             m->moments);
+    double mom[2 * (kIn + kOut)];
+    CUDA_TRY(cudaMemcpyAsync(mom, m->moments, sizeof(mom), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    float norm[2 * kIn + 2 * kOut];
+    for (int c = 0; c < kIn + kOut; ++c) {
+      const double mu = mom[c] / samples;
+      const double var = std::max(0.0, mom[kIn + kOut + c] / samples - mu * mu);
+      const float sd = (float)std::max(std::sqrt(var), 1e-6);
+      if (c < kIn) {
+        norm[c] = (float)mu;
+        norm[kIn + c] = sd;
+      } else {
+        norm[2 * kIn + (c - kIn)] = (float)mu;
+        norm[2 * kIn + kOut + (c - kIn)] = sd;
+      }
+    }
+    CUDA_TRY(cudaMemcpyAsync(m->blob + clsph_nn::kOffXMu, norm, sizeof(norm), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  const uint64_t per_epoch = samples / rows;
+  const uint64_t total = per_epoch * cfg->epochs;
+  if (total >= (1ull << 31)) return fail(CLSPH_ERR_ARGUMENT, "mlp_train: too many steps");
+  if ((rc = ensure_loss(m, (uint32_t)total))) return rc;
+  CUDA_TRY(cudaMemsetAsync(m->loss, 0, sizeof(float) * total, s));
+  std::vector<uint32_t> perm(samples);
+  std::mt19937_64 rng(cfg->seed);
+  const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+  uint64_t step = 0;
+  for (uint32_t e = 0; e < cfg->epochs; ++e) {
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::shuffle(perm.begin(), perm.end(), rng);
+    CUDA_TRY(cudaStreamSynchronize(s));  // the previous epoch's gathers read m->idx
+    CUDA_TRY(cudaMemcpyAsync(m->idx, perm.data(), sizeof(uint32_t) * samples, cudaMemcpyHostToDevice, s));
+    for (uint64_t b = 0; b < per_epoch; ++b, ++step) {
+      clsph_nn::k_gather_batch<<<(rows * (kIn + kOut) + 255) / 256, 256, 0, s>>>(
+          x_raw, y_raw, m->idx + b * rows, rows, m->blob + clsph_nn::kOffXMu, m->xb, m->yb);
+      if ((rc = pass(m, rows, m->loss + step, true))) return rc;
+      const float frac = total > 1 ? (float)step / (float)(total - 1) : 0.f;
+      const float lr = cfg->lr + (cfg->lr_final - cfg->lr) * frac;
+      ++m->adam_t;
+      const float bc1 = 1.f - std::pow(beta1, (float)m->adam_t);
+      const float bc2 = 1.f - std::pow(beta2, (float)m->adam_t);
+      clsph_nn::k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(m->blob, m->grad, m->adam_m, m->adam_v, kParams,
+                                                            lr, beta1, beta2, eps, bc1, bc2, bf16_weights(m));
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  std::vector<float> losses(total);
+  CUDA_TRY(cudaMemcpyAsync(losses.data(), m->loss, sizeof(float) * total, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t nlog = 0;
+  if (loss_log && log_len) {
+    const uint32_t every = std::max<uint32_t>(1, cfg->log_every);
+    for (uint64_t b0 = 0; b0 < total && nlog < log_len; b0 += every) {
+      const uint64_t b1 = std::min<uint64_t>(total, b0 + every);
+      double acc = 0.0;
+      for (uint64_t b = b0; b < b1; ++b) acc += losses[b];
+      loss_log[nlog++] = (float)(acc / (double)(b1 - b0) / rows);
+    }
+  }
+  if (logged) *logged = nlog;
+  return CLSPH_OK;
+}
+
+// ---- collector
+
+int clsph_collector_destroy(clsph_collector* c) {
+  if (!c) return CLSPH_OK;
+  if (c->h && c->h->stream) cudaStreamSynchronize(c->h->stream);
+  void* bufs[] = {c->ring, c->xs, c->ys, c->scratch.pos, c->scratch.vel, c->scratch.ivel,
+                  c->zero, c->sbbox, c->sstatus, c->scapped};
+  for (void* b : bufs) cudaFree(b);
+  delete c;
+  return CLSPH_OK;
+}
+
+int clsph_collector_create(clsph_gpu* h, uint32_t id_stride, uint32_t dt_mult, uint64_t capacity,
+                           clsph_collector** out) {
+  if (!h || !out || id_stride == 0 || dt_mult == 0 || dt_mult > 64 || capacity == 0)
+    return fail(CLSPH_ERR_ARGUMENT, "collector_create: bad argument");
+  auto* c = new clsph_collector();
+  c->h = h;
+  c->stride = id_stride;
+  c->dt_mult = dt_mult;
+  c->m = (h->n + id_stride - 1) / id_stride;
+  c->capacity = capacity;
+  const size_t n = h->n;
+  int rc;
+  if ((rc = dev_alloc(&c->ring, (size_t)(dt_mult + 1) * c->m * kRing)) ||
+      (rc = dev_alloc(&c->xs, capacity * kFeat)) || (rc = dev_alloc(&c->ys, capacity * kOut)) ||
+      (rc = dev_alloc(&c->scratch.pos, n)) || (rc = dev_alloc(&c->scratch.vel, n)) ||
+      (rc = dev_alloc(&c->scratch.ivel, n)) || (rc = dev_alloc(&c->zero, n)) ||
+      (rc = dev_alloc(&c->sbbox, 6 * (size_t)h->nscenes)) || (rc = dev_alloc(&c->sstatus, 1)) ||
+      (rc = dev_alloc(&c->scapped, 1))) {
+    clsph_collector_destroy(c);
+    return rc;
+  }
+  if (cudaMemset(c->zero, 0, sizeof(float4) * n) != cudaSuccess ||
+      cudaMemset(c->sbbox, 0, sizeof(uint32_t) * 6 * h->nscenes) != cudaSuccess) {
+    clsph_collector_destroy(c);
+    return fail(CLSPH_ERR_CUDA, "collector_create: memset");
+  }
+  *out = c;
+  return CLSPH_OK;
+}
+
+int clsph_collector_step(clsph_collector* c, uint32_t substeps) {
+  if (!c) return fail(CLSPH_ERR_ARGUMENT, "collector_step: null collector");
+  clsph_gpu* h = c->h;
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "collector_step: upload particles first");
+  const uint32_t n = h->n;
+  const uint32_t levels = c->dt_mult + 1;
+  for (uint32_t k = 0; k < substeps; ++k) {
+    int rc = enqueue_substep(h, CLSPH_STAGE_DENSITY);
+    if (rc) return rc;
+    // forces (the plain kernel's accelerations) + the tracked particles' features
+    float* level = c->ring + (size_t)(c->t % levels) * c->m * kRing;
+    FeatureHook fh = feature_hook(h, kFeatRing);
+    fh.raw = level;
+    fh.ids = h->ids[h->ids_sel];
+    fh.stride = c->stride;
+    fh.m = c->m;
+    if ((rc = launch_forces_hooked(h, fh))) return rc;
+    // the naive dt_mult step from this state, into scratch
+    h->launch(K_MISC, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
+              dim3(kBlock), n, h->st[1], (const float4*)h->acc, c->scratch, (const DevMesh*)h->meshes,
+              (const Consts*)h->consts, (const uint16_t*)h->scene_of, h->max_iters, c->sbbox, c->sstatus,
+              c->scapped, (const float4*)c->zero, (float)c->dt_mult, position_weight(c->dt_mult));
+    h->launch(K_MISC, k_ring_naive, dim3(grid_blocks(n)), dim3(kBlock), n, (const uint32_t*)h->ids[h->ids_sel],
+              c->stride, c->m, (const float4*)c->scratch.ivel, (const Consts*)h->consts,
+              (const uint16_t*)h->scene_of, level);
+    if (c->t >= c->dt_mult && c->count < c->capacity) {
+      const float* old_level = c->ring + (size_t)((c->t - c->dt_mult) % levels) * c->m * kRing;
+      h->launch(K_MISC, k_sample, dim3((c->m + 255) / 256), dim3(256), old_level, (const float*)level, c->m,
+                1.f / (float)c->dt_mult, c->xs, c->ys, c->count, c->capacity);
+      c->count = std::min<uint64_t>(c->capacity, c->count + c->m);
+    }
+    if ((rc = enqueue_advect(h))) return rc;
+    ++h->substeps;
+    ++c->t;
+  }
+  if (substeps) h->have_fields = true;
+  return check_launch(h);
+}
+
+int clsph_collector_samples(clsph_collector* c, const float** x_raw, const float** y_raw, uint64_t* count) {
+  if (!c) return fail(CLSPH_ERR_ARGUMENT, "collector_samples: null collector");
+  CUDA_TRY(cudaStreamSynchronize(c->h->stream));
+  if (x_raw) *x_raw = c->xs;
+  if (y_raw) *y_raw = c->ys;
+  if (count) *count = c->count;
+  return CLSPH_OK;
+}
+
+int clsph_collector_copy(clsph_collector* c, float* x_host, float* y_host, uint64_t first, uint64_t count) {
+  if (!c || (count && (!x_host || !y_host))) return fail(CLSPH_ERR_ARGUMENT, "collector_copy: bad argument");
+  CUDA_TRY(cudaStreamSynchronize(c->h->stream));
+  if (first > c->count || count > c->count - first)
+    return fail(CLSPH_ERR_ARGUMENT, "collector_copy: range beyond the samples collected");
+  if (!count) return CLSPH_OK;
+  CUDA_TRY(cudaMemcpy(x_host, c->xs + first * kFeat, sizeof(float) * kFeat * count, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(y_host, c->ys + first * kOut, sizeof(float) * kOut * count, cudaMemcpyDeviceToHost));
+  return CLSPH_OK;
+}
+
+int clsph_gpu_read_features(clsph_gpu* h, float* features_host) {
+  if (!h || !features_host) return fail(CLSPH_ERR_ARGUMENT, "read_features: bad argument");
+  if (!h->have_fields) return fail(CLSPH_ERR_STATE, "read_features: run a substep to CLSPH_STAGE_FORCES first");
+  float* d = nullptr;
+  int rc = dev_alloc(&d, (size_t)h->n * kFeat);
+  if (rc) return rc;
+  FeatureHook fh = feature_hook(h, kFeatRaw);
+  fh.raw = d;
+  rc = launch_forces_hooked(h, fh);
+  if (rc) {
+    cudaFree(d);
+    return rc;
+  }
+  cudaError_t e = cudaMemcpyAsync(features_host, d, sizeof(float) * h->n * kFeat, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("read_features: ") + cudaGetErrorString(e));
+  return check_launch(h);
+}
+
+// ---- learned step
+
+int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const clsph_learned_config* cfg,
+                           clsph_learned_stats* stats) {
+  if (!h || !m || !cfg || cfg->dt_mult == 0 || cfg->dt_mult > 64 || !(cfg->threshold >= 0.f))
+    return fail(CLSPH_ERR_ARGUMENT, "step_learned: bad argument");
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step_learned: upload particles first");
+  if (m->device != h->device) return fail(CLSPH_ERR_ARGUMENT, "step_learned: MLP on another device");
+  LearnedCache* L = nullptr;
+  int rc = ensure_cache(h, &L);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(m->stream));  // weights in place
+  const uint32_t mult = cfg->dt_mult;
+  clsph_learned_stats st{};
+  int cur = 0;
+  bool pending = false;  // the last learned step awaits its density check; its input is snap[cur ^ 1]
+  uint32_t done = 0;
+  while (done < steps) {
+    if ((rc = save(h, L->snap[cur]))) return rc;
+    if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
+    if (pending && (rc = enqueue_gate(h, L))) return rc;
+    if ((rc = enqueue_learned_tail(h, m, L, mult))) return rc;
+    ++h->substeps;
+    if (pending) {
+      double dev = 0.0;
+      if ((rc = wait_gate(h, L, &dev))) return rc;
+      ++st.checks;
+      st.deviation_sum += dev;
+      st.deviation_max = std::max(st.deviation_max, dev);
+      if (!(dev <= cfg->threshold)) {
+        // roll the previous learned step back and cover its interval with plain substeps
+        if ((rc = restore(h, L->snap[cur ^ 1]))) return rc;
+        if ((rc = plain_substeps(h, mult))) return rc;
+        ++st.rejected;
+        st.plain_substeps += mult;
+        pending = false;
+        continue;
+      }
+      ++st.learned_steps;
+    }
+    pending = true;
+    ++done;
+    cur ^= 1;
+  }
+  if (pending) {
+    // check the last learned step with one neighbour build and density pass
+    if ((rc = save(h, L->snap[cur]))) return rc;
+    if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
+    if ((rc = enqueue_gate(h, L))) return rc;
+    double dev = 0.0;
+    if ((rc = wait_gate(h, L, &dev))) return rc;
+    if ((rc = restore(h, L->snap[cur]))) return rc;
+    ++st.checks;
+    st.deviation_sum += dev;
+    st.deviation_max = std::max(st.deviation_max, dev);
+    if (!(dev <= cfg->threshold)) {
+      if ((rc = restore(h, L->snap[cur ^ 1]))) return rc;
+      if ((rc = plain_substeps(h, mult))) return rc;
+      ++st.rejected;
+      st.plain_substeps += mult;
+    } else {
+      ++st.learned_steps;
+    }
+  }
+  h->have_fields = false;
+  if (stats) {
+    stats->learned_steps += st.learned_steps;
+    stats->rejected += st.rejected;
+    stats->plain_substeps += st.plain_substeps;
+    stats->checks += st.checks;
+    stats->deviation_sum += st.deviation_sum;
+    stats->deviation_max = std::max(stats->deviation_max, st.deviation_max);
+  }
+  return check_launch(h);
+}
+
+}  // extern "C"

@@ -67,7 +67,8 @@ class Settings:
 
 def derive(params: np.void, influence_count: int) -> tuple[np.void, np.void, float]:
     """Derived fields of sph_simulation.cpp:490-505 (see module docstring)."""
-    p = np.array(params, dtype=PARAMS).reshape(1).copy()
+    p = np.zeros(1, dtype=PARAMS)  # zeroed padding: the record is compared and passed as bytes
+    p[0] = params
     n = int(p["particles_count"][0])
     m = f32(p["particle_mass"][0])
     total_mass = f32(f32(n) * m)

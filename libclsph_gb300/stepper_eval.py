@@ -1,0 +1,135 @@
+"""Judges the learned 4x-dt stepper against the plain solver.
+
+Both runs start from the same state and cover the same simulated time
+(`plain_substeps` plain substeps = plain_substeps / dt_mult learned steps).
+Timing runs measure simulated seconds per wall second on the GPU; accuracy
+runs (the same deterministic trajectories, downloaded at checkpoints) compare
+the two states particle by particle (persistent ids):
+
+  density_dev_mean   mean over particles of |rho_L - rho_P| / rho0
+  density_dev_pop    |mean rho_L - mean rho_P| / rho0
+  rho_dev_plain/learned  mean |rho / rho0 - 1| of each run
+  pos_rms_h          RMS distance between a particle's two positions, in h
+  ke_plain/learned   kinetic energy
+
+Densities are those of the checkpoint state itself (one neighbour build and
+density pass on a scratch handle). No counterpart in the reference.
+"""
+
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import learned as Lm
+from .gpu import STAGE_DENSITY, GpuSolver
+
+
+def state_density(scratch: GpuSolver, state: np.ndarray) -> np.ndarray:
+    """Density of every slot of `state` (the plain density kernel on a scratch handle)."""
+    scratch.upload(state)
+    scratch.step_until(STAGE_DENSITY)
+    rho_sorted = scratch.fields()[0]
+    _, perm = scratch.keys()
+    rho = np.empty_like(rho_sorted)
+    rho[perm] = rho_sorted
+    return rho
+
+
+def by_id(solver: GpuSolver, scratch: GpuSolver):
+    state = solver.download()
+    ids = solver.ids()
+    order = np.argsort(ids)
+    rho = state_density(scratch, state)
+    return state[order], rho[order]
+
+
+def compare(p_state, p_rho, l_state, l_rho, params) -> dict:
+    rho0 = float(params["fluid_density"])
+    h = float(params["h"])
+    m = float(params["particle_mass"])
+    dpos = l_state["position"][:, :3].astype(np.float64) - p_state["position"][:, :3]
+    ke = lambda s: 0.5 * m * float((s["velocity"][:, :3].astype(np.float64) ** 2).sum())
+    return {
+        "density_dev_mean": float(np.abs(l_rho.astype(np.float64) - p_rho).mean() / rho0),
+        "density_dev_pop": float(abs(l_rho.astype(np.float64).mean() - p_rho.astype(np.float64).mean()) / rho0),
+        "rho_dev_plain": float(np.abs(p_rho / rho0 - 1).mean()),
+        "rho_dev_learned": float(np.abs(l_rho / rho0 - 1).mean()),
+        "pos_rms_h": float(np.sqrt((dpos ** 2).sum(1).mean()) / h),
+        "ke_plain": ke(p_state),
+        "ke_learned": ke(l_state),
+    }
+
+
+def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, checkpoints: int = 10,
+             threshold: float = 0.01, graph: bool = True) -> dict:
+    import torch
+
+    if plain_substeps % (dt_mult * checkpoints):
+        raise ValueError("plain_substeps must be a multiple of dt_mult * checkpoints")
+    learned_steps = plain_substeps // dt_mult
+    dt = float(np.float32(scene.params["time_delta"]) * np.float32(scene.params["simulation_scale"]))
+    sim_time = plain_substeps * dt
+
+    def solver():
+        s = GpuSolver(scene.params, scene.terms, scene.n, scene.mesh)
+        s.upload(scene.particles)
+        return s
+
+    # ---- timing: the whole interval, wall clock around synchronised runs
+    with solver() as p:
+        p.set_graph(graph)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p.step(plain_substeps)
+        p.sync()
+        plain_s = time.perf_counter() - t0
+    with solver() as lr:
+        stats = Lm.LearnedStats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Lm.step_learned(lr, mlp, learned_steps, dt_mult, threshold, stats)
+        lr.sync()
+        learned_s = time.perf_counter() - t0
+    # ---- accuracy: the same trajectories with checkpoints
+    curve = []
+    with solver() as p, solver() as lr, solver() as scratch:
+        p.set_graph(graph)
+        chk_stats = Lm.LearnedStats()
+        per = plain_substeps // checkpoints
+        for c in range(checkpoints):
+            p.step(per)
+            Lm.step_learned(lr, mlp, per // dt_mult, dt_mult, threshold, chk_stats)
+            ps, prho = by_id(p, scratch)
+            ls, lrho = by_id(lr, scratch)
+            row = compare(ps, prho, ls, lrho, scene.params)
+            row["t"] = (c + 1) * per * dt
+            curve.append(row)
+    st = stats.as_dict()
+    out = {
+        "workload": scene.name,
+        "particles": scene.n,
+        "dt_mult": dt_mult,
+        "threshold": threshold,
+        "plain_substeps": plain_substeps,
+        "learned_steps": learned_steps,
+        "sim_time_s": sim_time,
+        "plain_wall_s": plain_s,
+        "learned_wall_s": learned_s,
+        "plain_sim_s_per_s": sim_time / plain_s,
+        "learned_sim_s_per_s": sim_time / learned_s,
+        "speedup": plain_s / learned_s,
+        "plain_particle_steps_per_s": scene.n * plain_substeps / plain_s,
+        "fallback_fraction": st["fallback_fraction"],
+        "accepted_steps": st["learned_steps"],
+        "rejected_steps": st["rejected"],
+        "check_deviation_mean": st["deviation_mean"],
+        "check_deviation_max": st["deviation_max"],
+        "density_dev_mean": float(np.mean([r["density_dev_mean"] for r in curve])),
+        "density_dev_pop": float(np.mean([r["density_dev_pop"] for r in curve])),
+        "density_dev_mean_final": curve[-1]["density_dev_mean"],
+        "pos_rms_h_final": curve[-1]["pos_rms_h"],
+        "curve": curve,
+    }
+    return out

@@ -163,26 +163,29 @@ def dam_break_1m(seed: int = 1) -> Scene:
 def batched_dam_breaks(count: int = 256, seed: int = 5, n_min: int = 2048, n_max: int = 65536,
                        steps: int = 1000) -> list:
     """`count` independent dam breaks: particle count log-uniform in
-    [n_min, n_max], box edge 1 m * (N / 32768)^(1/3) (12 triangles), rest
-    density uniform in [900, 1200] kg/m^3, viscosity uniform in [0.5, 4] x
-    water's, m = 0.05 kg, lattice spacing h/2 with seeded jitter (the
-    32,768-particle scene scaled to each count)."""
+    [n_min, n_max], rest density uniform in [900, 1200] kg/m^3, viscosity
+    uniform in [0.5, 4] x water's. Each is the large dam break scaled to its
+    count: a 2:2:1 block (lattice spacing h/2, h = 1/64 m through the particle
+    mass, seeded jitter, top layer ragged) in the left quarter of a box four
+    block-widths long, two high and four deep (12 triangles)."""
     rng = np.random.default_rng(seed)
+    h = 1.0 / 64.0
+    s = h / 2
     out = []
     for k in range(count):
         n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
         rho0 = float(rng.uniform(900.0, 1200.0))
         mu = float(WATER["dynamic_viscosity"] * rng.uniform(0.5, 4.0))
-        st = water_settings(n, fluid_density=rho0, dynamic_viscosity=mu)
-        h = float(st.params["h"])
-        s = h / 2
-        edge = (n / 32768.0) ** (1.0 / 3.0)
-        side = int(math.ceil(n ** (1.0 / 3.0)))
-        block = lattice((side, side, side), s, (0.0, 0.0, 0.0), 0.01, rng)[:n]
-        block += np.float32((edge - side * s) / 2)  # centred in its box
+        st = water_settings(n, mass=mass_for_h(h, rho0), fluid_density=rho0, dynamic_viscosity=mu)
+        side = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
+        dims = (2 * side, 2 * side, side)
+        block = lattice(dims, s, (0.0, 0.0, 0.0), 0.01, rng)
+        # fill the block layer by layer from the floor: sort by height, keep n
+        block = block[np.argsort(block[:, 1], kind="stable")][:n]
+        box = (4 * dims[0] * s, 2 * dims[1] * s, 4 * dims[2] * s)
         out.append(Scene(f"batched_{k}", st.params, st.terms, particles_from_arrays(block),
-                         box_mesh((0, 0, 0), (edge, edge, edge)), steps,
-                         {"h": h, "rho0": rho0, "mu": mu, "edge": edge, "seed": seed}))
+                         box_mesh((0, 0, 0), box), steps,
+                         {"h": float(st.params["h"]), "rho0": rho0, "mu": mu, "box": box, "seed": seed}))
     return out
 
 

@@ -38,6 +38,21 @@ def test_gpu_library_exports_header_symbols():
     assert sorted(s[0] for s in SIGNATURES) == names
 
 
+def test_gpu_library_exports_learned_symbols():
+    header = ROOT / "include" / "clsph_learned.h"
+    names = sorted(set(declared(header, "clsph_mlp_") + declared(header, "clsph_collector_") +
+                       declared(header, "clsph_gpu_")) - set(declared(ROOT / "include" / "clsph_gpu.h", "clsph_gpu_")))
+    assert len(names) >= 15
+    lib = ctypes.CDLL(str(GPU_SO))
+    for n in names:
+        assert hasattr(lib, n), n
+    from libclsph_gb300.learned import BLOB, SIGNATURES
+
+    assert sorted(s[0] for s in SIGNATURES) == names
+    lib.clsph_mlp_blob_size.restype = ctypes.c_uint64
+    assert lib.clsph_mlp_blob_size() == BLOB == 75268 + 72
+
+
 def test_host_library_exports():
     lib = ctypes.CDLL(str(HOST_SO))
     for n in ("clsph_host_load_settings", "clsph_host_scene_new", "clsph_host_scene_load",
