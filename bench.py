@@ -22,8 +22,10 @@ triangles), synthetic and seeded.
 oracle port; the OpenCL CPU device is unavailable on these hosts) on a
 65,536-particle sample of the same workload per step, all host threads.
 
-Multi-GPU: the substep does not shard; N ranks run N independent replicas
-(weak scaling, no collective on the data path).
+Multi-GPU: a single scene does not shard (no halo exchange is built), so N
+ranks run N independent replicas of it (weak scaling); the batched workload
+splits its scenes over the ranks by particle count (strong scaling). There is
+no collective on the data path, only the barrier and the timing reductions.
 """
 
 from __future__ import annotations
@@ -85,9 +87,15 @@ class Batch:
         return len(self.particles)
 
 
-def load_workload(name):
+def load_workload(name, world: int = 1, rank: int = 0):
+    """The workload of this rank: a replica of a single scene, or this rank's
+    share of a batch's scenes."""
     w = WORKLOADS[name]()
-    return Batch(w) if isinstance(w, list) else w
+    if isinstance(w, list):
+        if world > 1:
+            w = [w[k] for k in partition_scenes([s.n for s in w], world)[rank]]
+        return Batch(w)
+    return w
 
 
 def make_solver(scene):
@@ -172,37 +180,56 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def dist_setup():
+def dist_setup(backend: str | None = None):
+    """Rank, world size and local rank from the torchrun environment; one
+    process per GPU over NCCL (gloo on hosts without CUDA). The ranks only
+    meet for the barrier and the timing reductions: each one runs its own
+    replica (or its own share of a batch's scenes) with no collective on the
+    data path."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
 
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
     return world, rank, local
 
 
-def max_over_ranks(x: float, world: int) -> float:
+def _reduce(x: float, world: int, op: str) -> float:
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    return _reduce(x, world, "max")
 
 
 def sum_over_ranks(x: float, world: int) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
+    return _reduce(x, world, "sum")
 
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t)
-    return float(t.item())
+
+def partition_scenes(sizes, world: int) -> list[list[int]]:
+    """Scenes of a batch split over ranks by particle count (longest first to
+    the least-loaded rank); every scene on exactly one rank."""
+    loads = [0] * world
+    parts: list[list[int]] = [[] for _ in range(world)]
+    for k in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda q: (loads[q], q))
+        parts[r].append(k)
+        loads[r] += sizes[k]
+    return [sorted(p) for p in parts]
 
 
 def barrier(world: int) -> None:
@@ -294,7 +321,7 @@ def run_reference(args, world, rank) -> None:
         "impl": "reference", "metric": "particle-steps/s", "value": value,
         "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "strong" if isinstance(scene, Batch) else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": scene.name, "n_particles": sample_n, "full_n_particles": scene.n},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{sample_n} of the {scene.n} particles (same spacing, mass, "
@@ -324,13 +351,15 @@ def learned_evaluation(scene, solver) -> dict | None:
     r = evaluate(scene, mlp, plain_substeps=2000, dt_mult=4, checkpoints=10, threshold=0.01)
     mlp.close()
     keep = ("plain_sim_s_per_s", "learned_sim_s_per_s", "speedup", "fallback_fraction", "accepted_steps",
-            "rejected_steps", "check_deviation_mean", "check_deviation_max", "density_dev_mean",
-            "density_dev_pop", "density_dev_mean_final", "pos_rms_h_final", "threshold", "dt_mult",
+            "rejected_steps", "check_deviation_mean", "check_deviation_max", "density_dev",
+            "density_dev_max", "density_dev_pop", "density_dev_particle", "rho_dev_plain",
+            "rho_dev_learned", "pos_rms_h_final", "pos_rms_chaos_h_final", "density_dev_chaos", "threshold", "dt_mult",
             "plain_substeps", "learned_steps", "sim_time_s")
     out = {k: r[k] for k in keep}
     out["curve_t"] = [c["t"] for c in r["curve"]]
-    out["curve_density_dev_mean"] = [c["density_dev_mean"] for c in r["curve"]]
+    out["curve_density_dev"] = [c["density_dev"] for c in r["curve"]]
     out["curve_pos_rms_h"] = [c["pos_rms_h"] for c in r["curve"]]
+    out["curve_pos_rms_chaos_h"] = [c["pos_rms_chaos_h"] for c in r["curve"]]
     out["curve_ke_plain"] = [c["ke_plain"] for c in r["curve"]]
     out["curve_ke_learned"] = [c["ke_learned"] for c in r["curve"]]
     return out
@@ -365,7 +394,7 @@ def main() -> None:
 
     torch.cuda.set_device(local)
     load_library()
-    scene = load_workload(args.workload)
+    scene = load_workload(args.workload, world, rank)
     n = scene.n
     log(f"[rank {rank}] {scene.name}: n={n}")
     stream = torch.cuda.Stream()
@@ -477,7 +506,7 @@ def main() -> None:
         "warmup": args.warmup,
         "ms_per_step": 1e3 * device_s_max / args.steps,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if isinstance(scene, Batch) else "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",

@@ -14,23 +14,28 @@
  *   - the learned step: one neighbour build, density and force evaluation
  *     (the plain kernels), the MLP's acceleration correction, and one
  *     advection/collision pass over dt_mult plain time steps. The MLP also
- *     predicts each particle's density after the step; the next step's
- *     density pass compares it with the density actually reached, and when
- *     the mean |rho - rho_predicted| / rho0 exceeds the threshold the step is
- *     rolled back and replaced by dt_mult plain substeps (the plain solver is
- *     the fallback and the judge).
+ *     predicts the density each particle would reach under the plain solver.
+ *     The next step's density pass measures the predicted density deviation
+ *     of the step, max(|D - D_pred|, |M - M_pred|) over the particles with
+ *     D = mean |rho/rho0 - 1| and M = mean rho/rho0 of the densities reached
+ *     (rho) and predicted (rho_pred); above the threshold the step is rolled
+ *     back and replaced by dt_mult plain substeps (the plain solver is the
+ *     fallback and the judge).
  *
  * Features of particle i (h, dt = time_delta * simulation_scale, rho0, K and
  * vmax of its scene; sums over contributing neighbours j != i,
- * d = (x_j - x_i)/h, u = (v_j - v_i) dt/h with v the intermediate velocity,
- * w = 1 - |d|^2):
+ * d = (x_j - x_i)/h, u = (v_j - v_i) dt/h with v the particle velocity,
+ * w = 1 - |d|^2; neighbour count includes i):
  *   0 rho/rho0 - 1      1 p/K          2 neighbour count / 32
- *   3-5 a dt^2/h (plain acceleration)   6-8 v dt/h     9 |v|/vmax
+ *   3-5 a dt^2/h (plain acceleration)   6-8 v' dt/h and 9 |v'|/vmax with v'
+ *   the intermediate velocity
  *   10-12 sum w d       13-18 sum w d d^T (xx yy zz xy xz yz)
  *   19-21 sum w u       22-27 sum w u u^T   28 sum w d.u   29-31 sum w d x u
  * Outputs: 0-2 acceleration correction in units h/dt^2, 3 relative density
  * change over the step. Inputs and outputs are standardised with the
- * sample set's mean and standard deviation (stored with the weights).
+ * sample set's mean and standard deviation (stored with the weights);
+ * standardised inputs are clamped to +-6 and, in the learned step, each
+ * output to its mean +- 4 standard deviations.
  *
  * Parameter blob (floats): W1[32][256] b1[256] W2[256][256] b2[256]
  * W3[256][4] b3[4] x_mu[32] x_sigma[32] y_mu[4] y_sigma[4]; W stored
@@ -66,7 +71,7 @@ int clsph_mlp_get_blob(clsph_mlp* m, float* blob, uint64_t count);
  * tensor-core wait. */
 int clsph_mlp_forward(clsph_mlp* m, const uint16_t* x_bf16, uint32_t rows, float* y, void* cuda_stream);
 /* The same network on the warp-level mma.sync path (a cross-check of the
- * tcgen05 kernel; layer 3 with BF16 weights). */
+ * tcgen05 kernel). */
 int clsph_mlp_forward_mma_sync(clsph_mlp* m, const uint16_t* x_bf16, uint32_t rows, float* y,
                                void* cuda_stream);
 /* De-standardised predictions y_host[rows][4] (host) for raw device feature
@@ -115,6 +120,11 @@ int clsph_collector_destroy(clsph_collector* c);
  * recording one sample per tracked particle per substep once dt_mult
  * substeps of history exist. */
 int clsph_collector_step(clsph_collector* c, uint32_t substeps);
+/* `steps` learned steps of h with network m (no density check), recording at
+ * every visited state the samples of the plain solver's outcome from it
+ * (dt_mult plain substeps from a snapshot, then back): training data from
+ * the states the learned stepper itself reaches. */
+int clsph_collector_step_learned(clsph_collector* c, clsph_mlp* m, uint32_t steps);
 /* Device pointers to the samples so far (x [count][32], y [count][4]). */
 int clsph_collector_samples(clsph_collector* c, const float** x_raw, const float** y_raw,
                             uint64_t* count);
@@ -129,22 +139,33 @@ int clsph_gpu_read_features(clsph_gpu* h, float* features_host);
 
 typedef struct {
   uint32_t dt_mult;  /* plain time steps per learned step (4) */
-  float threshold;   /* rollback when mean |rho - rho_predicted| / rho0 exceeds this (0.01) */
+  float threshold;   /* rollback when the predicted density deviation exceeds this (0.01) */
+  uint32_t flags;    /* CLSPH_LEARNED_CALIBRATE: calibrate the check on fallback intervals */
 } clsph_learned_config;
+
+enum { CLSPH_LEARNED_CALIBRATE = 1 };
 
 typedef struct {
   uint64_t learned_steps;  /* accepted learned steps */
   uint64_t rejected;       /* learned steps rolled back */
   uint64_t plain_substeps; /* substeps run as fallback */
   uint64_t checks;         /* density checks made */
-  double deviation_sum;    /* sum of the checked mean deviations */
+  double deviation_sum;    /* sum of the checked predicted density deviations */
   double deviation_max;
+  double particle_deviation_sum; /* sum of the checked mean |rho - rho_pred| / rho0 */
+  double calibration_d;  /* current calibration of D_pred and M_pred (see below) */
+  double calibration_m;
 } clsph_learned_stats;
 
 /* Advances h by `steps` x dt_mult plain time steps, each as one learned step
  * when it passes the density check, else as dt_mult plain substeps. The last
  * learned step is checked with one extra neighbour build and density pass.
- * stats (may be NULL) is accumulated, not cleared. */
+ * With CLSPH_LEARNED_CALIBRATE every fallback interval also calibrates the
+ * check: the plain statistics it reaches, minus those the network predicted
+ * for it, update an exponential average b (weight 0.3) that is added to
+ * D_pred and M_pred of later checks (the calibration belongs to the handle
+ * and restarts when another network is passed). stats (may be NULL) is
+ * accumulated, not cleared. */
 int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const clsph_learned_config* cfg,
                            clsph_learned_stats* stats);
 

@@ -742,7 +742,8 @@ __global__ void __launch_bounds__(BLOCK)
 struct NoForceHook {
   struct Acc {};
   __device__ __forceinline__ Acc begin(uint32_t) const { return {}; }
-  __device__ __forceinline__ void pair(Acc&, uint32_t, uint32_t, const float4&, const float4&) const {}
+  __device__ __forceinline__ void pair(Acc&, uint32_t, uint32_t, const float4&, const float4&,
+                                       const float4&) const {}
   __device__ __forceinline__ void end(Acc&, uint32_t, const float4&) const {}
 };
 
@@ -772,8 +773,9 @@ __global__ void __launch_bounds__(BLOCK)
     const float4 pj = __ldg(&st.pos[j]);
     const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
     const float rr = xnorm(d);
-    force_pair(f, j == i, d, rr, vi, __ldg(&st.vel[j]), __ldg(&aux[j]), own, hh, lap_b, c);
-    hook.pair(ha, i, j, pi, pj);
+    const float4 vj = __ldg(&st.vel[j]);
+    force_pair(f, j == i, d, rr, vi, vj, __ldg(&aux[j]), own, hh, lap_b, c);
+    hook.pair(ha, i, j, pi, pj, vj);
   };
   const uint32_t cnt = ncount[i];
   if (cnt <= nlist_cap) {

@@ -60,7 +60,7 @@ struct FeatureHook {
   uint32_t stride, m;
 
   struct Acc {
-    float inv_h, vs, vx, vy, vz;
+    float inv_h, vs, vx, vy, vz;  // vx..vz: the particle's velocity (pair moments)
     float s[22];  // sum w d (3), w d d^T (6), w u (3), w u u^T (6), w d.u, w d x u (3)
     uint32_t cnt;
   };
@@ -70,7 +70,7 @@ struct FeatureHook {
     const Consts& c = consts[scene_of[i]];
     a.inv_h = 1.f / c.h;
     a.vs = c.time_delta * c.scale * a.inv_h;
-    const float4 v = st.ivel[i];
+    const float4 v = st.vel[i];
     a.vx = v.x;
     a.vy = v.y;
     a.vz = v.z;
@@ -80,10 +80,11 @@ struct FeatureHook {
     return a;
   }
 
-  __device__ __forceinline__ void pair(Acc& a, uint32_t i, uint32_t j, const float4& pi, const float4& pj) const {
+  // vj: the neighbour's velocity, already loaded by the force evaluation
+  __device__ __forceinline__ void pair(Acc& a, uint32_t i, uint32_t j, const float4& pi, const float4& pj,
+                                       const float4& vj) const {
     ++a.cnt;
     if (j == i) return;
-    const float4 vj = __ldg(&st.ivel[j]);
     const float dx = (pj.x - pi.x) * a.inv_h, dy = (pj.y - pi.y) * a.inv_h, dz = (pj.z - pi.z) * a.inv_h;
     const float ux = (vj.x - a.vx) * a.vs, uy = (vj.y - a.vy) * a.vs, uz = (vj.z - a.vz) * a.vs;
     const float w = fmaxf(0.f, 1.f - (dx * dx + dy * dy + dz * dz));
@@ -130,10 +131,11 @@ struct FeatureHook {
     f[3] = acc.x * as;
     f[4] = acc.y * as;
     f[5] = acc.z * as;
-    f[6] = a.vx * a.vs;
-    f[7] = a.vy * a.vs;
-    f[8] = a.vz * a.vs;
-    f[9] = c.vmax > 0.f ? sqrtf(a.vx * a.vx + a.vy * a.vy + a.vz * a.vz) / c.vmax : 0.f;
+    const float4 vh = st.ivel[i];  // the intermediate velocity the step integrates
+    f[6] = vh.x * a.vs;
+    f[7] = vh.y * a.vs;
+    f[8] = vh.z * a.vs;
+    f[9] = c.vmax > 0.f ? sqrtf(vh.x * vh.x + vh.y * vh.y + vh.z * vh.z) / c.vmax : 0.f;
 #pragma unroll
     for (int k = 0; k < 22; ++k) f[10 + k] = a.s[k];
     if (mode == kFeatStd) {
@@ -144,8 +146,8 @@ struct FeatureHook {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int k = qq * 8 + 2 * e;
-          w[e] = clsph_nn::pack_bf16((f[k] - norm[k]) / norm[kFeat + k],
-                                      (f[k + 1] - norm[k + 1]) / norm[kFeat + k + 1]);
+          w[e] = clsph_nn::pack_bf16(clsph_nn::standardise(f[k], norm[k], norm[kFeat + k]),
+                                      clsph_nn::standardise(f[k + 1], norm[k + 1], norm[kFeat + k + 1]));
         }
         row[qq] = make_uint4(w[0], w[1], w[2], w[3]);
       }
@@ -195,37 +197,61 @@ __global__ void k_sample(const float* __restrict__ old_level, const float* __res
   ys[s * kOut + 3] = (w[0] + 1.f) / (o[0] + 1.f) - 1.f;
 }
 
-// sum over particles of |rho - rho_predicted| / rho0 (predicted density in vel.w)
+// Density statistics of the state just evaluated against the densities the
+// network predicted for it (vel.w): sums over particles of
+//   [0] |rho/rho0 - 1|   [1] |rho_pred/rho0 - 1|   [2] rho/rho0   [3] rho_pred/rho0
+//   [4] |rho - rho_pred| / rho0
+constexpr int kGateSums = 5;
 __global__ void __launch_bounds__(kBlock)
     k_gate(uint32_t n, const float4* __restrict__ aux, const float4* __restrict__ vel,
            const Consts* __restrict__ consts, const uint16_t* __restrict__ scene_of,
-           float* __restrict__ dev_sum) {
-  __shared__ float red[kBlock / 32];
-  float s = 0.f;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    s += fabsf(aux[i].x - vel[i].w) / consts[scene_of[i]].rho0;
+           float* __restrict__ sums) {
+  __shared__ float red[kGateSums][kBlock / 32];
+  float s[kGateSums] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float inv = 1.f / consts[scene_of[i]].rho0;
+    const float r = aux[i].x * inv, rp = vel[i].w * inv;
+    s[0] += fabsf(r - 1.f);
+    s[1] += fabsf(rp - 1.f);
+    s[2] += r;
+    s[3] += rp;
+    s[4] += fabsf(r - rp);
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  for (int k = 0; k < kGateSums; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = s[k];
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < kGateSums) {
     float t = 0.f;
-    for (int w = 0; w < kBlock / 32; ++w) t += red[w];
-    atomicAdd(dev_sum, t);
+    for (int w = 0; w < kBlock / 32; ++w) t += red[threadIdx.x][w];
+    atomicAdd(&sums[threadIdx.x], t);
   }
 }
 
-// MLP outputs -> physical acceleration correction and predicted density
+// MLP outputs -> physical acceleration correction and predicted density.
+// Each output is first clamped to its training mean +- kOutputClamp standard
+// deviations, which bounds the correction a single step can apply.
+constexpr float kOutputClamp = 4.f;
 struct StoreCorr {
   float4* corr;
   const float4* aux;
   const Consts* consts;
   const uint16_t* scene_of;
+  const float* y_mu;     // [4]
+  const float* y_sigma;  // [4]
+  __device__ float clamp_out(float v, int k) const {
+    const float lo = y_mu[k] - kOutputClamp * y_sigma[k], hi = y_mu[k] + kOutputClamp * y_sigma[k];
+    return fminf(fmaxf(v, lo), hi);
+  }
   __device__ void operator()(uint32_t row, float4 y) const {
     const Consts& c = consts[scene_of[row]];
     const float dt = c.time_delta * c.scale;
     const float s = c.h / (dt * dt);
-    corr[row] = make_float4(y.x * s, y.y * s, y.z * s, aux[row].x * (1.f + y.w));
+    corr[row] = make_float4(clamp_out(y.x, 0) * s, clamp_out(y.y, 1) * s, clamp_out(y.z, 2) * s,
+                            aux[row].x * (1.f + clamp_out(y.w, 3)));
   }
 };
 
@@ -316,6 +342,7 @@ struct clsph_mlp {
   bf16* w3b = nullptr;    // [256][8]
   bf16* w1t = nullptr;    // [256][32]
   bf16* w2t = nullptr;    // [256][256]
+  bf16* w3t = nullptr;    // [16][256]
   uint32_t* err = nullptr;  // tensor-core wait timeouts of clsph_mlp_forward
   // training state, made on first use
   uint32_t rows_cap = 0;
@@ -335,13 +362,13 @@ struct clsph_mlp {
 namespace {
 
 clsph_nn::Bf16Weights bf16_weights(const clsph_mlp* m) {
-  return clsph_nn::Bf16Weights{m->w1b, m->w2b, m->w3b, m->w1t, m->w2t};
+  return clsph_nn::Bf16Weights{m->w1b, m->w2b, m->w3b, m->w1t, m->w2t, m->w3t};
 }
 
 clsph_nn::TcWeights tc_weights(const clsph_mlp* m) {
   return clsph_nn::TcWeights{m->w1t,
                              m->w2t,
-                             m->blob + clsph_nn::kOffW3,
+                             m->w3t,
                              m->blob + clsph_nn::kOffB1,
                              m->blob + clsph_nn::kOffB2,
                              m->blob + clsph_nn::kOffB3,
@@ -479,6 +506,7 @@ int pass(clsph_mlp* m, uint32_t rows, float* loss_slot, bool backward) {
 
 int refresh_bf16(clsph_mlp* m) {
   clsph_nn::k_refresh_bf16<<<(kParams + 255) / 256, 256, 0, m->stream>>>(m->blob, bf16_weights(m));
+  static_assert(kParams > 16 * kHid, "refresh grid covers the W3 padding");
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -495,9 +523,15 @@ struct LearnedCache {
   bf16* x = nullptr;       // [n][32]
   float4* corr = nullptr;  // [n]
   Snapshot snap[2];
-  float* dev_sum = nullptr;   // [0] deviation sum, [1] tensor-core error word
-  float* dev_host = nullptr;  // pinned copy of both
+  float* dev_sum = nullptr;   // [0..4] gate sums, [5] tensor-core error word
+  float* dev_host = nullptr;  // pinned copy
   cudaEvent_t ev = nullptr;
+  // online calibration of the predicted density statistics against the plain
+  // substeps run as fallback (exponential average of plain - predicted)
+  const clsph_mlp* calibrated_for = nullptr;
+  double bias_d = 0.0, bias_m = 0.0;
+  bool calib_pending = false;        // a fallback interval awaits its plain statistics
+  double rejected_d = 0.0, rejected_m = 0.0;  // predictions for that interval
 };
 
 void free_cache(clsph_gpu* h) {
@@ -529,14 +563,14 @@ int ensure_cache(clsph_gpu* h, LearnedCache** out) {
   h->free_learned = free_cache;
   const size_t n = h->n;
   int rc;
-  if ((rc = dev_alloc(&L->x, n * kFeat)) || (rc = dev_alloc(&L->corr, n)) || (rc = dev_alloc(&L->dev_sum, 2)))
+  if ((rc = dev_alloc(&L->x, n * kFeat)) || (rc = dev_alloc(&L->corr, n)) || (rc = dev_alloc(&L->dev_sum, kGateSums + 1)))
     return rc;
-  CUDA_TRY(cudaMemset(L->dev_sum, 0, 2 * sizeof(float)));
+  CUDA_TRY(cudaMemset(L->dev_sum, 0, (kGateSums + 1) * sizeof(float)));
   for (auto& s : L->snap)
     if ((rc = dev_alloc(&s.pos, n)) || (rc = dev_alloc(&s.vel, n)) || (rc = dev_alloc(&s.ivel, n)) ||
         (rc = dev_alloc(&s.ids, n)) || (rc = dev_alloc(&s.bbox, 6 * (size_t)h->nscenes)))
       return rc;
-  CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), 2 * sizeof(float)));
+  CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), (kGateSums + 1) * sizeof(float)));
   CUDA_TRY(cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming));
   *out = L;
   return 0;
@@ -568,25 +602,47 @@ int restore(clsph_gpu* h, const Snapshot& s) {
   return 0;
 }
 
-// density check of the state just sorted and evaluated: mean |rho - rho_pred| / rho0
+// density check of the state just sorted and evaluated
 int enqueue_gate(clsph_gpu* h, LearnedCache* L) {
-  CUDA_TRY(cudaMemsetAsync(L->dev_sum, 0, sizeof(float), h->stream));
+  CUDA_TRY(cudaMemsetAsync(L->dev_sum, 0, kGateSums * sizeof(float), h->stream));
   h->launch(K_GATE, k_gate, dim3(grid_blocks(h->n, h->sm_count * 4)), dim3(kBlock), h->n,
             (const float4*)h->aux, (const float4*)h->st[1].vel, (const Consts*)h->consts,
             (const uint16_t*)h->scene_of, L->dev_sum);
-  CUDA_TRY(cudaMemcpyAsync(L->dev_host, L->dev_sum, 2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(L->dev_host, L->dev_sum, (kGateSums + 1) * sizeof(float), cudaMemcpyDeviceToHost,
+                           h->stream));
   CUDA_TRY(cudaEventRecord(L->ev, h->stream));
   return 0;
 }
 
-int wait_gate(clsph_gpu* h, LearnedCache* L, double* dev) {
+// Density statistics read back by enqueue_gate: D = mean |rho/rho0 - 1| and
+// M = mean rho/rho0 of the state just evaluated, D_pred and M_pred of the
+// densities predicted for it, P = mean |rho - rho_pred| / rho0.
+struct GateStats {
+  double d, d_pred, m, m_pred, particle;
+};
+
+int wait_gate(clsph_gpu* h, LearnedCache* L, GateStats* g) {
   CUDA_TRY(cudaEventSynchronize(L->ev));
   uint32_t errw;
-  std::memcpy(&errw, L->dev_host + 1, sizeof(errw));
+  std::memcpy(&errw, L->dev_host + kGateSums, sizeof(errw));
   if (errw) return fail(CLSPH_ERR_CUDA, "step_learned: a tensor-core wait of the MLP kernel timed out");
-  *dev = (double)L->dev_host[0] / (double)h->n;
+  const double inv = 1.0 / (double)h->n;
+  g->d = L->dev_host[0] * inv;
+  g->d_pred = L->dev_host[1] * inv;
+  g->m = L->dev_host[2] * inv;
+  g->m_pred = L->dev_host[3] * inv;
+  g->particle = L->dev_host[4] * inv;
   return 0;
 }
+
+// The predicted density deviation of a learned step: how far the density
+// statistics it reached lie from those predicted for the plain solver (after
+// the calibration), max(|D - D_pred - b_D|, |M - M_pred - b_M|).
+double predicted_deviation(const GateStats& g, const LearnedCache* L) {
+  return std::max(std::fabs(g.d - g.d_pred - L->bias_d), std::fabs(g.m - g.m_pred - L->bias_m));
+}
+
+constexpr double kCalibrationWeight = 0.3;
 
 // forces + features -> MLP -> one advection over dt_mult time steps
 int enqueue_learned_tail(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t dt_mult) {
@@ -597,7 +653,8 @@ int enqueue_learned_tail(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t d
   int rc = launch_forces_hooked(h, fh);
   if (rc) return rc;
   rc = launch_tc(h->stream, h->sm_count, L->x, n, tc_weights(m),
-                     StoreCorr{L->corr, h->aux, h->consts, h->scene_of},
+                     StoreCorr{L->corr, h->aux, h->consts, h->scene_of, m->blob + clsph_nn::kOffYMu,
+                               m->blob + clsph_nn::kOffYSigma},
                      reinterpret_cast<uint32_t*>(L->dev_sum + 1), h, K_MLP);
   if (rc) return rc;
   h->launch(K_LEARNED_ADVECT, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
@@ -642,7 +699,7 @@ uint64_t clsph_mlp_blob_size(void) { return kBlob; }
 int clsph_mlp_destroy(clsph_mlp* m) {
   if (!m) return CLSPH_OK;
   if (m->stream) cudaStreamSynchronize(m->stream);
-  void* bufs[] = {m->blob, m->w1b, m->w2b, m->w3b, m->w1t,  m->w2t,    m->err,    m->grad,
+  void* bufs[] = {m->blob, m->w1b, m->w2b, m->w3b, m->w1t,  m->w2t,    m->w3t,    m->err,    m->grad,
                   m->adam_m, m->adam_v, m->xb, m->h1, m->h2, m->dz1, m->dz2, m->yb, m->z1, m->z2,
                   m->ws,   m->loss, m->idx, m->moments};
   for (void* b : bufs) cudaFree(b);
@@ -670,7 +727,7 @@ int clsph_mlp_create(uint64_t seed, clsph_mlp** out) {
   int rc;
   if ((rc = alloc(&m->blob, kBlob)) || (rc = alloc(&m->w1b, kIn * kHid)) || (rc = alloc(&m->w2b, kHid * kHid)) ||
       (rc = alloc(&m->w3b, kHid * kOutPad)) || (rc = alloc(&m->w1t, kIn * kHid)) ||
-      (rc = alloc(&m->w2t, kHid * kHid)) || (rc = alloc(&m->err, 1)))
+      (rc = alloc(&m->w2t, kHid * kHid)) || (rc = alloc(&m->w3t, 16 * kHid)) || (rc = alloc(&m->err, 1)))
     return bail(rc);
   if (cudaMemset(m->err, 0, sizeof(uint32_t)) != cudaSuccess) return bail(fail(CLSPH_ERR_CUDA, "mlp_create: memset"));
   std::vector<float> blob(kBlob, 0.f);
@@ -934,42 +991,87 @@ int clsph_collector_create(clsph_gpu* h, uint32_t id_stride, uint32_t dt_mult, u
   return CLSPH_OK;
 }
 
+namespace {
+
+// Density, forces and the tracked particles' ring entry (features and the
+// naive dt_mult step's velocity) of the handle's current state; leaves the
+// substep ready for its advection.
+int collect_level(clsph_collector* c, float* level) {
+  clsph_gpu* h = c->h;
+  const uint32_t n = h->n;
+  int rc = enqueue_substep(h, CLSPH_STAGE_DENSITY);
+  if (rc) return rc;
+  FeatureHook fh = feature_hook(h, kFeatRing);
+  fh.raw = level;
+  fh.ids = h->ids[h->ids_sel];
+  fh.stride = c->stride;
+  fh.m = c->m;
+  if ((rc = launch_forces_hooked(h, fh))) return rc;
+  h->launch(K_MISC, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)), dim3(kBlock),
+            n, h->st[1], (const float4*)h->acc, c->scratch, (const DevMesh*)h->meshes, (const Consts*)h->consts,
+            (const uint16_t*)h->scene_of, h->max_iters, c->sbbox, c->sstatus, c->scapped,
+            (const float4*)c->zero, (float)c->dt_mult, position_weight(c->dt_mult));
+  h->launch(K_MISC, k_ring_naive, dim3(grid_blocks(n)), dim3(kBlock), n, (const uint32_t*)h->ids[h->ids_sel],
+            c->stride, c->m, (const float4*)c->scratch.ivel, (const Consts*)h->consts,
+            (const uint16_t*)h->scene_of, level);
+  return 0;
+}
+
+void emit_samples(clsph_collector* c, const float* old_level, const float* level) {
+  if (c->count >= c->capacity) return;
+  c->h->launch(K_MISC, k_sample, dim3((c->m + 255) / 256), dim3(256), old_level, level, c->m,
+               1.f / (float)c->dt_mult, c->xs, c->ys, c->count, c->capacity);
+  c->count = std::min<uint64_t>(c->capacity, c->count + c->m);
+}
+
+}  // namespace
+
 int clsph_collector_step(clsph_collector* c, uint32_t substeps) {
   if (!c) return fail(CLSPH_ERR_ARGUMENT, "collector_step: null collector");
   clsph_gpu* h = c->h;
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "collector_step: upload particles first");
-  const uint32_t n = h->n;
   const uint32_t levels = c->dt_mult + 1;
   for (uint32_t k = 0; k < substeps; ++k) {
-    int rc = enqueue_substep(h, CLSPH_STAGE_DENSITY);
-    if (rc) return rc;
-    // forces (the plain kernel's accelerations) + the tracked particles' features
     float* level = c->ring + (size_t)(c->t % levels) * c->m * kRing;
-    FeatureHook fh = feature_hook(h, kFeatRing);
-    fh.raw = level;
-    fh.ids = h->ids[h->ids_sel];
-    fh.stride = c->stride;
-    fh.m = c->m;
-    if ((rc = launch_forces_hooked(h, fh))) return rc;
-    // the naive dt_mult step from this state, into scratch
-    h->launch(K_MISC, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
-              dim3(kBlock), n, h->st[1], (const float4*)h->acc, c->scratch, (const DevMesh*)h->meshes,
-              (const Consts*)h->consts, (const uint16_t*)h->scene_of, h->max_iters, c->sbbox, c->sstatus,
-              c->scapped, (const float4*)c->zero, (float)c->dt_mult, position_weight(c->dt_mult));
-    h->launch(K_MISC, k_ring_naive, dim3(grid_blocks(n)), dim3(kBlock), n, (const uint32_t*)h->ids[h->ids_sel],
-              c->stride, c->m, (const float4*)c->scratch.ivel, (const Consts*)h->consts,
-              (const uint16_t*)h->scene_of, level);
-    if (c->t >= c->dt_mult && c->count < c->capacity) {
-      const float* old_level = c->ring + (size_t)((c->t - c->dt_mult) % levels) * c->m * kRing;
-      h->launch(K_MISC, k_sample, dim3((c->m + 255) / 256), dim3(256), old_level, (const float*)level, c->m,
-                1.f / (float)c->dt_mult, c->xs, c->ys, c->count, c->capacity);
-      c->count = std::min<uint64_t>(c->capacity, c->count + c->m);
-    }
+    int rc = collect_level(c, level);
+    if (rc) return rc;
+    if (c->t >= c->dt_mult)
+      emit_samples(c, c->ring + (size_t)((c->t - c->dt_mult) % levels) * c->m * kRing, level);
     if ((rc = enqueue_advect(h))) return rc;
     ++h->substeps;
     ++c->t;
   }
   if (substeps) h->have_fields = true;
+  return check_launch(h);
+}
+
+int clsph_collector_step_learned(clsph_collector* c, clsph_mlp* m, uint32_t steps) {
+  if (!c || !m) return fail(CLSPH_ERR_ARGUMENT, "collector_step_learned: bad argument");
+  clsph_gpu* h = c->h;
+  if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "collector_step_learned: upload particles first");
+  if (m->device != h->device) return fail(CLSPH_ERR_ARGUMENT, "collector_step_learned: MLP on another device");
+  LearnedCache* L = nullptr;
+  int rc = ensure_cache(h, &L);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  float* lv0 = c->ring;
+  float* lv1 = c->ring + (size_t)c->m * kRing;
+  for (uint32_t k = 0; k < steps; ++k) {
+    // the plain outcome of the visited state: dt_mult substeps, features at both ends
+    if ((rc = save(h, L->snap[0]))) return rc;
+    if ((rc = collect_level(c, lv0)) || (rc = enqueue_advect(h))) return rc;
+    for (uint32_t q = 1; q < c->dt_mult; ++q)
+      if ((rc = enqueue_substep(h, CLSPH_STAGE_ADVECT))) return rc;
+    if ((rc = collect_level(c, lv1))) return rc;
+    emit_samples(c, lv0, lv1);
+    // back to the visited state, then one learned step onward
+    if ((rc = restore(h, L->snap[0]))) return rc;
+    if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
+    if ((rc = enqueue_learned_tail(h, m, L, c->dt_mult))) return rc;
+    h->substeps += 1;
+  }
+  c->t = 0;  // the plain-trajectory ring restarts after this
+  h->have_fields = false;
   return check_launch(h);
 }
 
@@ -1024,30 +1126,57 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
   LearnedCache* L = nullptr;
   int rc = ensure_cache(h, &L);
   if (rc) return rc;
+  if (L->calibrated_for != m || !(cfg->flags & CLSPH_LEARNED_CALIBRATE)) {
+    L->calibrated_for = m;
+    L->bias_d = L->bias_m = 0.0;
+    L->calib_pending = false;
+  }
   CUDA_TRY(cudaStreamSynchronize(m->stream));  // weights in place
   const uint32_t mult = cfg->dt_mult;
   clsph_learned_stats st{};
+  auto record = [&](const GateStats& g, double dev) {
+    ++st.checks;
+    st.deviation_sum += dev;
+    st.particle_deviation_sum += g.particle;
+    st.deviation_max = std::max(st.deviation_max, dev);
+  };
+  // roll the learned step whose input is `snap` back, redo its interval with
+  // plain substeps and calibrate on their result at the next density pass
+  auto fall_back = [&](const Snapshot& snap, const GateStats& g) -> int {
+    int r;
+    if ((r = restore(h, snap))) return r;
+    if ((r = plain_substeps(h, mult))) return r;
+    ++st.rejected;
+    st.plain_substeps += mult;
+    L->calib_pending = true;
+    L->rejected_d = g.d_pred;
+    L->rejected_m = g.m_pred;
+    return 0;
+  };
   int cur = 0;
   bool pending = false;  // the last learned step awaits its density check; its input is snap[cur ^ 1]
   uint32_t done = 0;
   while (done < steps) {
     if ((rc = save(h, L->snap[cur]))) return rc;
     if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
-    if (pending && (rc = enqueue_gate(h, L))) return rc;
+    const bool calib = !pending && L->calib_pending && (cfg->flags & CLSPH_LEARNED_CALIBRATE);
+    if ((pending || calib) && (rc = enqueue_gate(h, L))) return rc;
     if ((rc = enqueue_learned_tail(h, m, L, mult))) return rc;
     ++h->substeps;
+    if (calib) {
+      GateStats g;
+      if ((rc = wait_gate(h, L, &g))) return rc;
+      L->bias_d += kCalibrationWeight * ((g.d - L->rejected_d) - L->bias_d);
+      L->bias_m += kCalibrationWeight * ((g.m - L->rejected_m) - L->bias_m);
+      L->calib_pending = false;
+    }
     if (pending) {
-      double dev = 0.0;
-      if ((rc = wait_gate(h, L, &dev))) return rc;
-      ++st.checks;
-      st.deviation_sum += dev;
-      st.deviation_max = std::max(st.deviation_max, dev);
+      GateStats g;
+      if ((rc = wait_gate(h, L, &g))) return rc;
+      const double dev = predicted_deviation(g, L);
+      record(g, dev);
       if (!(dev <= cfg->threshold)) {
-        // roll the previous learned step back and cover its interval with plain substeps
-        if ((rc = restore(h, L->snap[cur ^ 1]))) return rc;
-        if ((rc = plain_substeps(h, mult))) return rc;
-        ++st.rejected;
-        st.plain_substeps += mult;
+        if ((rc = fall_back(L->snap[cur ^ 1], g))) return rc;
         pending = false;
         continue;
       }
@@ -1062,17 +1191,13 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
     if ((rc = save(h, L->snap[cur]))) return rc;
     if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
     if ((rc = enqueue_gate(h, L))) return rc;
-    double dev = 0.0;
-    if ((rc = wait_gate(h, L, &dev))) return rc;
+    GateStats g;
+    if ((rc = wait_gate(h, L, &g))) return rc;
     if ((rc = restore(h, L->snap[cur]))) return rc;
-    ++st.checks;
-    st.deviation_sum += dev;
-    st.deviation_max = std::max(st.deviation_max, dev);
+    const double dev = predicted_deviation(g, L);
+    record(g, dev);
     if (!(dev <= cfg->threshold)) {
-      if ((rc = restore(h, L->snap[cur ^ 1]))) return rc;
-      if ((rc = plain_substeps(h, mult))) return rc;
-      ++st.rejected;
-      st.plain_substeps += mult;
+      if ((rc = fall_back(L->snap[cur ^ 1], g))) return rc;
     } else {
       ++st.learned_steps;
     }
@@ -1084,7 +1209,10 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
     stats->plain_substeps += st.plain_substeps;
     stats->checks += st.checks;
     stats->deviation_sum += st.deviation_sum;
+    stats->particle_deviation_sum += st.particle_deviation_sum;
     stats->deviation_max = std::max(stats->deviation_max, st.deviation_max);
+    stats->calibration_d = L->bias_d;
+    stats->calibration_m = L->bias_m;
   }
   return check_launch(h);
 }

@@ -92,6 +92,14 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
+// Standardised inputs are clamped to +-kInputClamp (training and inference
+// alike): states outside the training distribution cannot drive the network
+// into extrapolation.
+constexpr float kInputClamp = 6.f;
+__device__ __forceinline__ float standardise(float v, float mu, float sigma) {
+  return fminf(fmaxf((v - mu) / sigma, -kInputClamp), kInputClamp);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);
@@ -466,7 +474,7 @@ __global__ void k_gather_batch(const float* __restrict__ x_raw, const float* __r
   if (r >= rows) return;
   const size_t s = idx[r];
   if (c < kIn) {
-    const float v = (x_raw[s * kIn + c] - norm[c]) / norm[kIn + c];
+    const float v = standardise(x_raw[s * kIn + c], norm[c], norm[kIn + c]);
     xb[(size_t)r * kIn + c] = __float2bfloat16_rn(v);
   } else {
     const int k = c - kIn;
@@ -480,7 +488,7 @@ __global__ void k_standardize(const float* __restrict__ x_raw, uint32_t rows, co
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (size_t)rows * kIn) return;
   const int c = (int)(i % kIn);
-  xb[i] = __float2bfloat16_rn((x_raw[i] - norm[c]) / norm[kIn + c]);
+  xb[i] = __float2bfloat16_rn(standardise(x_raw[i], norm[c], norm[kIn + c]));
 }
 
 // Layer 3 forward + loss + backward to dZ2, one block of 256 threads (one per
@@ -496,9 +504,9 @@ __global__ void __launch_bounds__(kHid)
   __shared__ float red[kHid / 32][kOut];
   __shared__ float dy_s[kOut];
   const int k = threadIdx.x, lane = k & 31, warp = k >> 5;
-  float w[kOut];
+  float w[kOut];  // BF16 values, as the inference kernels use them
 #pragma unroll
-  for (int j = 0; j < kOut; ++j) w[j] = w3[k * kOut + j];
+  for (int j = 0; j < kOut; ++j) w[j] = __bfloat162float(__float2bfloat16_rn(w3[k * kOut + j]));
   float gw[kOut] = {}, gb[kOut] = {}, lsum = 0.f;
   const uint32_t r_begin = blockIdx.x * rows_per_block;
   const uint32_t r_end = min(rows, r_begin + rows_per_block);
@@ -575,6 +583,7 @@ struct Bf16Weights {
   bf16* w3;
   bf16* w1t;
   bf16* w2t;
+  bf16* w3t;  // [16][256], rows 4..15 zero
   __device__ void put(int i, float v) const {
     const bf16 b = __float2bfloat16_rn(v);
     if (i < kOffB1) {
@@ -587,6 +596,7 @@ struct Bf16Weights {
     } else if (i >= kOffW3 && i < kOffB3) {
       const int j = i - kOffW3;
       w3[(j / kOut) * kOutPad + j % kOut] = b;
+      w3t[(j % kOut) * kHid + j / kOut] = b;
     }
   }
 };
@@ -612,6 +622,7 @@ __global__ void k_refresh_bf16(const float* __restrict__ p, Bf16Weights wb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < kParams) wb.put(i, p[i]);
   if (i < kHid * kOutPad && i % kOutPad >= kOut) wb.w3[i] = __float2bfloat16_rn(0.f);
+  if (i >= kOut * kHid && i < 16 * kHid) wb.w3t[i] = __float2bfloat16_rn(0.f);
 }
 
 // Standardisation statistics of the sample set: sums of x, x^2 (cols

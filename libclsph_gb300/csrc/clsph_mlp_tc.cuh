@@ -1,17 +1,19 @@
 // Fused MLP inference on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// One persistent CTA per SM, 128-row tiles. Both weight matrices live in
-// shared memory for the whole launch (W2 128 KB, W1 16 KB, canonical
-// no-swizzle K-major core-matrix layout); accumulators live in tensor memory
-// (layer 1 in columns 0..255, layer 2 in columns 256..511 of a 512-column
-// allocation). Per tile:
-//   all threads   X rows -> shared memory (A operand of layer 1)
+// One persistent CTA of 16 warps per SM, 128-row tiles. All three weight
+// matrices live in shared memory for the whole launch (W2 128 KB, W1 16 KB,
+// W3 padded to 16 outputs 8 KB; canonical no-swizzle K-major core-matrix
+// layout); accumulators live in tensor memory (layer 1 and layer 3 in
+// columns 0..255, layer 2 in columns 256..511 of a 512-column allocation).
+// Per tile:
+//   all threads   X rows (loaded into registers during the previous tile's
+//                 layer-2 MMAs) -> shared memory, the A operand of layer 1
 //   thread 0      2 x tcgen05.mma M128 N256 K16 -> TMEM, tcgen05.commit -> mbarrier
-//   8 warps       tcgen05.ld, + b1, GELU, BF16 -> shared memory (A operand of layer 2)
-//   thread 0      16 x tcgen05.mma M128 N256 K16 -> TMEM, commit
-//   8 warps       tcgen05.ld, + b2, GELU, layer 3 (256 -> 4, FP32 W3) on the CUDA
-//                 cores, the two column halves summed through shared memory,
-//                 de-standardised and handed to the Store hook.
+//   16 warps      tcgen05.ld, + b1, GELU, BF16 -> shared memory (A of layer 2)
+//   thread 0      16 x tcgen05.mma M128 N256 K16, commit
+//   16 warps      tcgen05.ld, + b2, GELU, BF16 -> shared memory (A of layer 3)
+//   thread 0      16 x tcgen05.mma M128 N16 K16, commit
+//   4 warps       tcgen05.ld of the 4 outputs, + b3, de-standardised, Store hook.
 // Every mbarrier wait is bounded; a wait that runs out sets *err, the CTA
 // leaves its tile loop, waits (bounded) for its own MMAs and frees TMEM.
 //
@@ -29,31 +31,34 @@
 namespace clsph_nn {
 
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;
 constexpr uint32_t kTcCols = 512;
+constexpr int kOut3 = 16;  // layer-3 MMA width (4 outputs, 12 zero columns)
 // shared-memory map (bytes)
 constexpr uint32_t kTcW2 = 0;                            // 256 x 256 bf16, SBO 4096
-constexpr uint32_t kTcH = kTcW2 + kHid * kHid * 2;       // 128 x 256 bf16, SBO 4096
+constexpr uint32_t kTcH = kTcW2 + kHid * kHid * 2;       // 128 x 256 bf16, SBO 4096 (H1, then H2)
 constexpr uint32_t kTcW1 = kTcH + kTcRows * kHid * 2;    // 256 x 32 bf16, SBO 512
 constexpr uint32_t kTcX = kTcW1 + kHid * kIn * 2;        // 128 x 32 bf16, SBO 512
-constexpr uint32_t kTcW3 = kTcX + kTcRows * kIn * 2;     // fp32 [256][4]
-constexpr uint32_t kTcB1 = kTcW3 + kHid * kOut * 4;      // fp32 [256]
+constexpr uint32_t kTcW3 = kTcX + kTcRows * kIn * 2;     // 16 x 256 bf16, SBO 4096
+constexpr uint32_t kTcB1 = kTcW3 + kOut3 * kHid * 2;     // fp32 [256]
 constexpr uint32_t kTcB2 = kTcB1 + kHid * 4;             // fp32 [256]
-constexpr uint32_t kTcRed = kTcB2 + kHid * 4;            // fp32 [128][4]
-constexpr uint32_t kTcMisc = kTcRed + kTcRows * kOut * 4;  // b3, y_mu, y_sigma [4 each]
+constexpr uint32_t kTcMisc = kTcB2 + kHid * 4;           // b3, y_mu, y_sigma [4 each]
 constexpr uint32_t kTcBar = kTcMisc + 48;                // mbarrier (8 B)
 constexpr uint32_t kTcSlot = kTcBar + 8;                 // TMEM base address (4 B)
 constexpr uint32_t kTcSmem = kTcSlot + 8;
 static_assert(kTcSmem <= 232448, "shared memory of the tcgen05 MLP");
 
-constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) |
-                              ((uint32_t)(kTcRows >> 4) << 24);
+constexpr uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+constexpr uint32_t kTcIdesc = tc_idesc(kTcRows, kHid);
+constexpr uint32_t kTcIdesc3 = tc_idesc(kTcRows, kOut3);
 constexpr uint32_t kTcWaitLimit = 1u << 24;
 
 struct TcWeights {
   const bf16* w1t;  // [256][32]  (W1 transposed: output-major, K contiguous)
   const bf16* w2t;  // [256][256] (W2 transposed)
-  const float* w3;  // [256][4]
+  const bf16* w3t;  // [16][256]  (W3 transposed, rows 4..15 zero)
   const float* b1;
   const float* b2;
   const float* b3;
@@ -121,10 +126,44 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 4 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
                "r"(v.w)
                : "memory");
+}
+
+// TMEM columns [col0, col0 + 64) of this thread's row -> + bias, GELU, BF16
+// -> the row's K slice of the canonical A-operand tile at `tile` (K = 256)
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, int col0, const float* bias, uint32_t tile,
+                                                   int r, const GeluConsts& gelu) {
+#pragma unroll 1
+  for (int c = 0; c < 2; ++c) {
+    const int cb = col0 + c * 32;
+    float v[32];
+    tc_ld32(taddr + cb, v);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      uint32_t p[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = e * 8 + 2 * q;
+        p[q] = gelu(v[k] + bias[cb + k], v[k + 1] + bias[cb + k + 1]);
+      }
+      st_shared_v4(tile + (r >> 3) * 4096 + ((cb + e * 8) >> 3) * 128 + (r & 7) * 16,
+                   make_uint4(p[0], p[1], p[2], p[3]));
+    }
+  }
 }
 
 template <class Store>
@@ -133,10 +172,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   const uint32_t sb = smem_addr(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float* s_w3 = reinterpret_cast<float*>(smem + kTcW3);
   float* s_b1 = reinterpret_cast<float*>(smem + kTcB1);
   float* s_b2 = reinterpret_cast<float*>(smem + kTcB2);
-  float* s_red = reinterpret_cast<float*>(smem + kTcRed);
   float* s_misc = reinterpret_cast<float*>(smem + kTcMisc);
   const uint32_t bar = sb + kTcBar;
 
@@ -144,15 +181,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // (row / 8) * SBO + (k / 8) * 128 + (row % 8) * 16 + (k % 8) * 2
   for (int q = tid; q < kHid * (kHid / 8); q += kTcThreads) {
     const int n = q >> 5, c = q & 31;
-    const uint4 v = reinterpret_cast<const uint4*>(w.w2t)[q];
-    st_shared_v4(sb + kTcW2 + (n >> 3) * 4096 + c * 128 + (n & 7) * 16, v);
+    st_shared_v4(sb + kTcW2 + (n >> 3) * 4096 + c * 128 + (n & 7) * 16, reinterpret_cast<const uint4*>(w.w2t)[q]);
   }
   for (int q = tid; q < kHid * (kIn / 8); q += kTcThreads) {
     const int n = q >> 2, c = q & 3;
-    const uint4 v = reinterpret_cast<const uint4*>(w.w1t)[q];
-    st_shared_v4(sb + kTcW1 + (n >> 3) * 512 + c * 128 + (n & 7) * 16, v);
+    st_shared_v4(sb + kTcW1 + (n >> 3) * 512 + c * 128 + (n & 7) * 16, reinterpret_cast<const uint4*>(w.w1t)[q]);
   }
-  for (int q = tid; q < kHid * kOut; q += kTcThreads) s_w3[q] = w.w3[q];
+  for (int q = tid; q < kOut3 * (kHid / 8); q += kTcThreads) {
+    const int n = q >> 5, c = q & 31;
+    st_shared_v4(sb + kTcW3 + (n >> 3) * 4096 + c * 128 + (n & 7) * 16, reinterpret_cast<const uint4*>(w.w3t)[q]);
+  }
   for (int q = tid; q < kHid; q += kTcThreads) {
     s_b1[q] = w.b1[q];
     s_b2[q] = w.b2[q];
@@ -178,25 +216,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + kTcSlot);
 
-  const int lg = warp & 3, half = warp >> 2;
+  const int lg = warp & 3, cq = warp >> 2;                      // lane quarter, column quarter
   const int r = lg * 32 + lane;                                  // tile row = TMEM lane
-  const uint32_t t_row = tmem + ((uint32_t)(lg * 32) << 16);     // this warp's lane quarter
-  const uint32_t k0 = pack_bf16(0.7978845608028654f, 0.7978845608028654f);
-  const uint32_t k01 = pack_bf16(0.7978845608028654f * 0.044715f, 0.7978845608028654f * 0.044715f);
-  const uint32_t hf = pack_bf16(0.5f, 0.5f);
+  const uint32_t t_row = tmem + ((uint32_t)(lg * 32) << 16);
+  const GeluConsts gelu;
   uint32_t phase = 0;
   bool ok = true;
   uint32_t issued = 0;  // commits made by thread 0 and not yet waited for
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
+  // this thread's 16-byte chunk of a tile's X rows: row tid / 4, chunk tid % 4
+  const int xr = tid >> 2, xc = tid & 3;
+  const uint32_t x_dst = sb + kTcX + (xr >> 3) * 512 + xc * 128 + (xr & 7) * 16;
+  auto load_x = [&](uint32_t tile) {
+    const uint32_t row = tile * kTcRows + xr;
+    return (tile < tiles && row < rows) ? reinterpret_cast<const uint4*>(x)[(size_t)row * (kIn / 8) + xc]
+                                        : make_uint4(0u, 0u, 0u, 0u);
+  };
+  auto wait_all = [&]() {
+    const bool got = tc_wait(bar, phase);
+    phase ^= 1;
+    if (tid == 0 && got) --issued;
+    return __syncthreads_and(got);
+  };
+  uint4 xv = load_x(blockIdx.x);
   for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
     const uint32_t row0 = tile * kTcRows;
-    for (int q = tid; q < kTcRows * (kIn / 8); q += kTcThreads) {
-      const int rr = q >> 2, c = q & 3;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (row0 + rr < rows) v = reinterpret_cast<const uint4*>(x)[(size_t)(row0 + rr) * (kIn / 8) + c];
-      st_shared_v4(sb + kTcX + (rr >> 3) * 512 + c * 128 + (rr & 7) * 16, v);
-    }
+    st_shared_v4(x_dst, xv);
     fence_async_smem();
+    tc_fence_before();
     __syncthreads();
     if (tid == 0) {
       tc_fence_after();
@@ -207,30 +254,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_commit(bar);
       ++issued;
     }
-    bool got = tc_wait(bar, phase);
-    phase ^= 1;
-    if (tid == 0 && got) --issued;
-    ok = __syncthreads_and(got);
-    if (!ok) break;
+    if (!(ok = wait_all())) break;
     tc_fence_after();
-    // layer-1 epilogue: 128 columns of this thread's row
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col0 = half * 128 + c * 32;
-      float v[32];
-      tc_ld32(t_row + col0, v);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        uint32_t p[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int k = e * 8 + 2 * q;
-          p[q] = gelu2_bf16(v[k] + s_b1[col0 + k], v[k + 1] + s_b1[col0 + k + 1], k0, k01, hf);
-        }
-        st_shared_v4(sb + kTcH + (r >> 3) * 4096 + ((col0 + e * 8) >> 3) * 128 + (r & 7) * 16,
-                     make_uint4(p[0], p[1], p[2], p[3]));
-      }
-    }
+    tc_hidden_epilogue(t_row, cq * 64, s_b1, sb + kTcH, r, gelu);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -243,40 +269,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_commit(bar);
       ++issued;
     }
-    got = tc_wait(bar, phase);
-    phase ^= 1;
-    if (tid == 0 && got) --issued;
-    ok = __syncthreads_and(got);
-    if (!ok) break;
+    xv = load_x(tile + gridDim.x);  // next tile's rows, in flight during the layer-2 MMAs
+    if (!(ok = wait_all())) break;
     tc_fence_after();
-    // layer-2 epilogue and layer 3
-    float y[kOut] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col0 = half * 128 + c * 32;
-      float v[32];
-      tc_ld32(t_row + 256 + col0, v);
-#pragma unroll
-      for (int k = 0; k < 32; k += 2) {
-        const uint32_t g = gelu2_bf16(v[k] + s_b2[col0 + k], v[k + 1] + s_b2[col0 + k + 1], k0, k01, hf);
-        const float g0 = __uint_as_float(g << 16), g1 = __uint_as_float(g & 0xFFFF0000u);
-        const float4 wa = reinterpret_cast<const float4*>(s_w3)[col0 + k];
-        const float4 wb = reinterpret_cast<const float4*>(s_w3)[col0 + k + 1];
-        y[0] += g0 * wa.x + g1 * wb.x;
-        y[1] += g0 * wa.y + g1 * wb.y;
-        y[2] += g0 * wa.z + g1 * wb.z;
-        y[3] += g0 * wa.w + g1 * wb.w;
-      }
-    }
-    if (half == 1) reinterpret_cast<float4*>(s_red)[r] = make_float4(y[0], y[1], y[2], y[3]);
+    tc_hidden_epilogue(t_row + 256, cq * 64, s_b2, sb + kTcH, r, gelu);
+    fence_async_smem();
     tc_fence_before();
     __syncthreads();
-    if (half == 0 && row0 + r < rows) {
-      const float4 o = reinterpret_cast<const float4*>(s_red)[r];
-      store(row0 + r, make_float4((y[0] + o.x + s_misc[0]) * s_misc[8] + s_misc[4],
-                                  (y[1] + o.y + s_misc[1]) * s_misc[9] + s_misc[5],
-                                  (y[2] + o.z + s_misc[2]) * s_misc[10] + s_misc[6],
-                                  (y[3] + o.w + s_misc[3]) * s_misc[11] + s_misc[7]));
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int ks = 0; ks < kHid / 16; ++ks)
+        tc_mma(tmem, tc_desc(sb + kTcH + ks * 256, 128, 4096), tc_desc(sb + kTcW3 + ks * 256, 128, 4096),
+               kTcIdesc3, ks > 0);
+      tc_commit(bar);
+      ++issued;
+    }
+    if (!(ok = wait_all())) break;
+    tc_fence_after();
+    if (cq == 0) {
+      float o[4];
+      tc_ld4(t_row, o);
+      if (row0 + r < rows)
+        store(row0 + r, make_float4((o[0] + s_misc[0]) * s_misc[8] + s_misc[4],
+                                    (o[1] + s_misc[1]) * s_misc[9] + s_misc[5],
+                                    (o[2] + s_misc[2]) * s_misc[10] + s_misc[6],
+                                    (o[3] + s_misc[3]) * s_misc[11] + s_misc[7]));
     }
   }
   // teardown: MMAs of this CTA must be complete before TMEM is freed

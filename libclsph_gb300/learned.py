@@ -51,17 +51,23 @@ class TrainConfig(ctypes.Structure):
                 ("seed", _u64), ("fit_normalisation", ctypes.c_int), ("log_every", _u32)]
 
 
+CALIBRATE = 1  # CLSPH_LEARNED_CALIBRATE
+
+
 class LearnedConfig(ctypes.Structure):
-    _fields_ = [("dt_mult", _u32), ("threshold", ctypes.c_float)]
+    _fields_ = [("dt_mult", _u32), ("threshold", ctypes.c_float), ("flags", _u32)]
 
 
 class LearnedStats(ctypes.Structure):
     _fields_ = [("learned_steps", _u64), ("rejected", _u64), ("plain_substeps", _u64), ("checks", _u64),
-                ("deviation_sum", ctypes.c_double), ("deviation_max", ctypes.c_double)]
+                ("deviation_sum", ctypes.c_double), ("deviation_max", ctypes.c_double),
+                ("particle_deviation_sum", ctypes.c_double), ("calibration_d", ctypes.c_double),
+                ("calibration_m", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_}
         d["deviation_mean"] = self.deviation_sum / self.checks if self.checks else 0.0
+        d["particle_deviation_mean"] = self.particle_deviation_sum / self.checks if self.checks else 0.0
         total = self.learned_steps + self.rejected
         d["fallback_fraction"] = self.rejected / total if total else 0.0
         return d
@@ -85,6 +91,7 @@ SIGNATURES = [
     ("clsph_collector_create", ctypes.c_int, [_vp, _u32, _u32, _u64, ctypes.POINTER(_vp)]),
     ("clsph_collector_destroy", ctypes.c_int, [_vp]),
     ("clsph_collector_step", ctypes.c_int, [_vp, _u32]),
+    ("clsph_collector_step_learned", ctypes.c_int, [_vp, _vp, _u32]),
     ("clsph_collector_samples", ctypes.c_int,
      [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_u64)]),
     ("clsph_collector_copy", ctypes.c_int, [_vp, _vp, _vp, _u64, _u64]),
@@ -220,6 +227,10 @@ class Collector:
     def step(self, substeps: int) -> None:
         _check(self.lib, "clsph_collector_step", self.lib.clsph_collector_step(self.h, substeps))
 
+    def step_learned(self, mlp: "Mlp", steps: int) -> None:
+        """Learned steps with `mlp`, recording the plain outcome of every visited state."""
+        _check(self.lib, "clsph_collector_step_learned", self.lib.clsph_collector_step_learned(self.h, mlp.h, steps))
+
     def samples(self) -> tuple[int, int, int]:
         """(x device pointer, y device pointer, count)."""
         x, y, n = _vp(), _vp(), _u64()
@@ -257,10 +268,10 @@ def read_features(solver: GpuSolver) -> np.ndarray:
 
 
 def step_learned(solver: GpuSolver, mlp: Mlp, steps: int, dt_mult: int = 4, threshold: float = 0.01,
-                 stats: LearnedStats | None = None) -> LearnedStats:
+                 stats: LearnedStats | None = None, calibrate: bool = False) -> LearnedStats:
     lib = library()
     st = stats if stats is not None else LearnedStats()
-    cfg = LearnedConfig(dt_mult, threshold)
+    cfg = LearnedConfig(dt_mult, threshold, CALIBRATE if calibrate else 0)
     _check(lib, "clsph_gpu_step_learned",
            lib.clsph_gpu_step_learned(solver.h, mlp.h, steps, ctypes.byref(cfg), ctypes.byref(st)))
     return st

@@ -4,12 +4,18 @@ Both runs start from the same state and cover the same simulated time
 (`plain_substeps` plain substeps = plain_substeps / dt_mult learned steps).
 Timing runs measure simulated seconds per wall second on the GPU; accuracy
 runs (the same deterministic trajectories, downloaded at checkpoints) compare
-the two states particle by particle (persistent ids):
+the two states:
 
-  density_dev_mean   mean over particles of |rho_L - rho_P| / rho0
+  rho_dev_plain/learned  mean |rho / rho0 - 1| of each run (the usual SPH
+                     density deviation; the headline `density_dev` is the
+                     mean over checkpoints of their difference)
   density_dev_pop    |mean rho_L - mean rho_P| / rho0
-  rho_dev_plain/learned  mean |rho / rho0 - 1| of each run
+  density_dev_particle  mean over particles (by id) of |rho_L - rho_P| / rho0
   pos_rms_h          RMS distance between a particle's two positions, in h
+  pos_rms_chaos_h, density_dev_chaos  the same measures between the plain
+                     run and a plain run whose initial positions differ by
+                     1e-6 h: how far two plain trajectories of this flow
+                     separate with no model error at all
   ke_plain/learned   kinetic energy
 
 Densities are those of the checkpoint state itself (one neighbour build and
@@ -51,11 +57,14 @@ def compare(p_state, p_rho, l_state, l_rho, params) -> dict:
     m = float(params["particle_mass"])
     dpos = l_state["position"][:, :3].astype(np.float64) - p_state["position"][:, :3]
     ke = lambda s: 0.5 * m * float((s["velocity"][:, :3].astype(np.float64) ** 2).sum())
+    d_p = float(np.abs(p_rho / rho0 - 1).mean())
+    d_l = float(np.abs(l_rho / rho0 - 1).mean())
     return {
-        "density_dev_mean": float(np.abs(l_rho.astype(np.float64) - p_rho).mean() / rho0),
+        "density_dev": abs(d_l - d_p),
+        "density_dev_particle": float(np.abs(l_rho.astype(np.float64) - p_rho).mean() / rho0),
         "density_dev_pop": float(abs(l_rho.astype(np.float64).mean() - p_rho.astype(np.float64).mean()) / rho0),
-        "rho_dev_plain": float(np.abs(p_rho / rho0 - 1).mean()),
-        "rho_dev_learned": float(np.abs(l_rho / rho0 - 1).mean()),
+        "rho_dev_plain": d_p,
+        "rho_dev_learned": d_l,
         "pos_rms_h": float(np.sqrt((dpos ** 2).sum(1).mean()) / h),
         "ke_plain": ke(p_state),
         "ke_learned": ke(l_state),
@@ -72,10 +81,15 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
     dt = float(np.float32(scene.params["time_delta"]) * np.float32(scene.params["simulation_scale"]))
     sim_time = plain_substeps * dt
 
-    def solver():
+    def solver(particles=None):
         s = GpuSolver(scene.params, scene.terms, scene.n, scene.mesh)
-        s.upload(scene.particles)
+        s.upload(scene.particles if particles is None else particles)
         return s
+
+    perturbed = scene.particles.copy()
+    rng = np.random.default_rng(12345)
+    eps = 1e-6 * float(scene.params["h"])
+    perturbed["position"][:, :3] += rng.uniform(-eps, eps, (scene.n, 3)).astype(np.float32)
 
     # ---- timing: the whole interval, wall clock around synchronised runs
     with solver() as p:
@@ -94,16 +108,23 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         learned_s = time.perf_counter() - t0
     # ---- accuracy: the same trajectories with checkpoints
     curve = []
-    with solver() as p, solver() as lr, solver() as scratch:
+    with solver() as p, solver() as lr, solver() as scratch, solver(perturbed) as pc:
         p.set_graph(graph)
+        pc.set_graph(graph)
         chk_stats = Lm.LearnedStats()
         per = plain_substeps // checkpoints
+        h = float(scene.params["h"])
         for c in range(checkpoints):
             p.step(per)
+            pc.step(per)
             Lm.step_learned(lr, mlp, per // dt_mult, dt_mult, threshold, chk_stats)
             ps, prho = by_id(p, scratch)
             ls, lrho = by_id(lr, scratch)
+            cs, crho = by_id(pc, scratch)
             row = compare(ps, prho, ls, lrho, scene.params)
+            chaos = compare(ps, prho, cs, crho, scene.params)
+            row["pos_rms_chaos_h"] = chaos["pos_rms_h"]
+            row["density_dev_chaos"] = chaos["density_dev"]
             row["t"] = (c + 1) * per * dt
             curve.append(row)
     st = stats.as_dict()
@@ -126,10 +147,16 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         "rejected_steps": st["rejected"],
         "check_deviation_mean": st["deviation_mean"],
         "check_deviation_max": st["deviation_max"],
-        "density_dev_mean": float(np.mean([r["density_dev_mean"] for r in curve])),
+        "density_dev": float(np.mean([r["density_dev"] for r in curve])),
+        "density_dev_max": float(np.max([r["density_dev"] for r in curve])),
         "density_dev_pop": float(np.mean([r["density_dev_pop"] for r in curve])),
-        "density_dev_mean_final": curve[-1]["density_dev_mean"],
+        "density_dev_particle": float(np.mean([r["density_dev_particle"] for r in curve])),
+        "rho_dev_plain": float(np.mean([r["rho_dev_plain"] for r in curve])),
+        "rho_dev_learned": float(np.mean([r["rho_dev_learned"] for r in curve])),
         "pos_rms_h_final": curve[-1]["pos_rms_h"],
+        "pos_rms_chaos_h_final": curve[-1]["pos_rms_chaos_h"],
+        "density_dev_chaos": float(np.mean([r["density_dev_chaos"] for r in curve])),
+        "check_particle_deviation_mean": st["particle_deviation_mean"],
         "curve": curve,
     }
     return out

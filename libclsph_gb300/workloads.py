@@ -164,10 +164,13 @@ def batched_dam_breaks(count: int = 256, seed: int = 5, n_min: int = 2048, n_max
                        steps: int = 1000) -> list:
     """`count` independent dam breaks: particle count log-uniform in
     [n_min, n_max], rest density uniform in [900, 1200] kg/m^3, viscosity
-    uniform in [0.5, 4] x water's. Each is the large dam break scaled to its
-    count: a 2:2:1 block (lattice spacing h/2, h = 1/64 m through the particle
-    mass, seeded jitter, top layer ragged) in the left quarter of a box four
-    block-widths long, two high and four deep (12 triangles)."""
+    uniform in [0.5, 4] x water's. Each is a water column released in a box
+    scaled to it: lattice spacing h/2 with h = 1/64 m (through the particle
+    mass) and seeded jitter, a column ny layers high (log-uniform in
+    [16, 128], i.e. up to the 1 m of the large dam break, which sets the
+    hydrostatic range the scenes cover) with an nx : nz = 2 : 1 footprint
+    (the large dam break's), top layer ragged, in the left quarter of a box
+    four columns long, twice its height and four columns deep (12 triangles)."""
     rng = np.random.default_rng(seed)
     h = 1.0 / 64.0
     s = h / 2
@@ -176,16 +179,20 @@ def batched_dam_breaks(count: int = 256, seed: int = 5, n_min: int = 2048, n_max
         n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
         rho0 = float(rng.uniform(900.0, 1200.0))
         mu = float(WATER["dynamic_viscosity"] * rng.uniform(0.5, 4.0))
+        ny = int(round(math.exp(rng.uniform(math.log(16), math.log(128)))))
+        nz = max(2, int(math.ceil(math.sqrt(n / (2.0 * ny)))))
+        nx = 2 * nz
+        ny = max(ny, int(math.ceil(n / (nx * nz))))
         st = water_settings(n, mass=mass_for_h(h, rho0), fluid_density=rho0, dynamic_viscosity=mu)
-        side = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
-        dims = (2 * side, 2 * side, side)
+        dims = (nx, ny, nz)
         block = lattice(dims, s, (0.0, 0.0, 0.0), 0.01, rng)
-        # fill the block layer by layer from the floor: sort by height, keep n
+        # fill the column layer by layer from the floor: sort by height, keep n
         block = block[np.argsort(block[:, 1], kind="stable")][:n]
-        box = (4 * dims[0] * s, 2 * dims[1] * s, 4 * dims[2] * s)
+        box = (4 * nx * s, 2 * ny * s, 4 * nz * s)
         out.append(Scene(f"batched_{k}", st.params, st.terms, particles_from_arrays(block),
                          box_mesh((0, 0, 0), box), steps,
-                         {"h": float(st.params["h"]), "rho0": rho0, "mu": mu, "box": box, "seed": seed}))
+                         {"h": float(st.params["h"]), "rho0": rho0, "mu": mu, "box": box,
+                          "dims": dims, "seed": seed}))
     return out
 
 
