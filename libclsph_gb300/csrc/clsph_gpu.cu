@@ -98,7 +98,7 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grids,
             (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
             (const uint32_t*)h->vals, h->st[0], h->st[1], (const uint32_t*)h->ids[src_ids],
-            h->ids[dst_ids], h->ci, h->cell_list, h->step_counters + kCntCells, h->hcode);
+            h->ids[dst_ids], h->ci, h->cell_list, h->step_counters + kCntCells);
   h->ids_sel = dst_ids;
   if (until <= CLSPH_STAGE_SORT) return 0;
   {
@@ -108,7 +108,7 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
       h->launch(K_DENSITY, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
                 (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
-                h->ncount, h->nlist_cap, (const uint8_t*)h->hcode);
+                h->ncount, h->nlist_cap);
     };
     if (b == 64) args(k_density<64>);
     else if (b == 256) args(k_density<256>);
@@ -351,8 +351,7 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
   while ((1u << log2s) < slots) ++log2s;
   if ((rc = dev_alloc(&h->aux, n)) || (rc = dev_alloc(&h->acc, n)) ||
       (rc = dev_alloc(&h->nlist, (size_t)h->nlist_cap * n)) || (rc = dev_alloc(&h->ncount, n)) ||
-      (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->hcode, n)) ||
-      (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
+      (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
       (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
       (rc = dev_alloc(&h->tile_hist, 256 * (size_t)h->ntiles)) ||
       (rc = dev_alloc(&h->digit_total, 4 * 256)) || (rc = dev_alloc(&h->ci.keys, slots)) ||
@@ -416,7 +415,7 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->st[s].ivel);
     cudaFree(h->ids[s]);
   }
-  void* bufs[] = {h->aux,      h->acc,      h->nlist,     h->ncount,      h->cell_list, h->hcode,
+  void* bufs[] = {h->aux,      h->acc,      h->nlist,     h->ncount,      h->cell_list,
                   h->step_counters, h->keys, h->vals,     h->tile_hist,   h->digit_total,
                   h->ci.keys,  h->ci.start, h->ci.end,    h->scene_of,    h->grids,
                   h->consts,   h->scene_h,  h->meshes,    h->bbox,        h->ctl,

@@ -129,7 +129,6 @@ struct clsph_gpu {
   uint32_t* ncount = nullptr;
   uint32_t nlist_cap = 64;
   uint32_t* cell_list = nullptr;      // first sorted slot of every occupied cell
-  uint8_t* hcode = nullptr;           // half code of every sorted slot
   uint32_t* step_counters = nullptr;  // kStepCounters, zeroed every substep
   uint32_t* keys = nullptr;           // [2n]
   uint32_t* vals = nullptr;           // [2n]

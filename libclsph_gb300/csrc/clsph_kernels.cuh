@@ -512,7 +512,7 @@ static __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
                          const uint32_t* __restrict__ vals_base, State src, State dst,
                          const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
                          CellIndex ci, uint32_t* __restrict__ cell_list,
-                         uint32_t* __restrict__ cell_count, uint8_t* __restrict__ hcode) {
+                         uint32_t* __restrict__ cell_count) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const KeySplit split{ctl[kCtlShift]};
@@ -522,10 +522,8 @@ static __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
   const uint32_t from = perm[s];
   const uint32_t key = keys[s];
   float4 p = src.pos[from];
-  const uint32_t code = half_code(p, split.morton(key), grids[scene_of[s]]);
-  p.w = __uint_as_float(code);
+  p.w = __uint_as_float(half_code(p, split.morton(key), grids[scene_of[s]]));
   dst.pos[s] = p;
-  hcode[s] = (uint8_t)code;
   dst.vel[s] = src.vel[from];
   dst.ivel[s] = src.ivel[from];
   ids_dst[s] = ids_src[from];
@@ -669,34 +667,19 @@ __device__ __forceinline__ uint32_t facing_mask(int ox, int oy, int oz) {
   return m;
 }
 
-// The half code of every sorted slot is also kept in a byte array, so a
-// candidate in a far half costs a 1-byte load instead of its 16-byte position.
 template <class F>
 __device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint32_t key,
                                                           uint32_t sbits, const CellIndex& ci,
-                                                          const float4* __restrict__ pos,
-                                                          const uint8_t* __restrict__ hcode, F&& f) {
+                                                          const float4* __restrict__ pos, F&& f) {
   const int c[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
   for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
     for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
       for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
         const uint32_t need = facing_mask((int)x - c[0], (int)y - c[1], (int)z - c[2]);
         const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
-        if (need == 0) {
-          for (uint32_t j = r.x; j < r.y; ++j) f(j, __ldg(&pos[j]));
-        } else {
-          // codes four at a time from 4-byte aligned words, in ascending slot order
-          uint32_t j = r.x;
-          for (; j < r.y && (j & 3u); ++j)
-            if ((__ldg(&hcode[j]) & need) == need) f(j, __ldg(&pos[j]));
-          for (; j + 4 <= r.y; j += 4) {
-            const uint32_t w4 = __ldg(reinterpret_cast<const uint32_t*>(hcode + j));
-#pragma unroll
-            for (uint32_t q = 0; q < 4; ++q)
-              if (((w4 >> (8 * q)) & need) == need) f(j + q, __ldg(&pos[j + q]));
-          }
-          for (; j < r.y; ++j)
-            if ((__ldg(&hcode[j]) & need) == need) f(j, __ldg(&pos[j]));
+        for (uint32_t j = r.x; j < r.y; ++j) {
+          const float4 pj = __ldg(&pos[j]);
+          if ((__float_as_uint(pj.w) & need) == need) f(j, pj);
         }
       }
 }
@@ -707,8 +690,7 @@ __global__ void __launch_bounds__(BLOCK)
               const uint32_t* __restrict__ ctl,
               const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos, CellIndex ci,
               const Consts* __restrict__ consts, float4* __restrict__ aux_out,
-              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap,
-              const uint8_t* __restrict__ hcode) {
+              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap) {
   __shared__ uint32_t cand[kScanCap][BLOCK];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -722,7 +704,7 @@ __global__ void __launch_bounds__(BLOCK)
   const Window w = neighbour_window(pi, key, grids[sc]);
   const float hh = XMUL(c.h, c.h);
   uint32_t found = 0;
-  for_each_facing_candidate(w, key, sbits, ci, pos, hcode, [&](uint32_t j, float4 pj) {
+  for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) {
       if (found < kScanCap) cand[found][threadIdx.x] = j;
@@ -746,7 +728,7 @@ __global__ void __launch_bounds__(BLOCK)
       visit(j, __ldg(&pos[j]));
     }
   } else {
-    for_each_facing_candidate(w, key, sbits, ci, pos, hcode, [&](uint32_t j, float4 pj) {
+    for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
       const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj);
     });
