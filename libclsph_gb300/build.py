@@ -66,7 +66,7 @@ def host_cmd() -> list[str]:
     srcs = sorted(str(p) for p in HOST.glob("*.cpp"))
     cuda_lib = Path(_nvcc()).resolve().parent.parent / "lib64"
     return [
-        os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared",
+        os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread",
         "-ffp-contract=off", f"-I{INCLUDE}", f"-I{INCLUDE / 'clsph'}", *srcs, "-o", str(HOST_SO),
         f"-L{LIB_DIR}", "-lclsph_gpu", "-Wl,-rpath,$ORIGIN", f"-L{cuda_lib}",
     ]

@@ -232,6 +232,27 @@ def test_houdini_writer_python_and_cpp_agree(tmp_path, host):
     assert a.rstrip().endswith("beginExtra\nendExtra")
 
 
+def test_houdini_writer_parallel_formatting_is_byte_identical(tmp_path, host):
+    """A frame large enough for the C++ writer's threaded formatting."""
+    rng = np.random.default_rng(4)
+    n = 20000
+    parts = np.zeros(n, dtype=PARTICLE)
+    parts["position"][:, :3] = rng.normal(0, 1, (n, 3))
+    parts["velocity"][:, :3] = rng.normal(0, 1, (n, 3))
+    parts["density"] = rng.uniform(0, 2200, n)
+    params = np.zeros(1, dtype=PARAMS)
+    params["particles_count"] = n
+    params["particle_mass"] = 0.05
+    (tmp_path / "py" / "frames").mkdir(parents=True)
+    (tmp_path / "cpp" / "frames").mkdir(parents=True)
+    HoudiniFileSaver(str(tmp_path / "py") + "/").writeFrameToFile(parts, params[0])
+    assert host.clsph_host_write_houdini((str(tmp_path / "cpp") + "/").encode(), parts.ctypes.data,
+                                         params.ctypes.data) == 0
+    a = (tmp_path / "py" / "frames" / "frame0000001.geo").read_bytes()
+    b = (tmp_path / "cpp" / "frames" / "frame0000001.geo").read_bytes()
+    assert a == b
+
+
 def test_frame_counter_naming(tmp_path):
     (tmp_path / "frames").mkdir()
     sv = HoudiniFileSaver(str(tmp_path) + "/")
