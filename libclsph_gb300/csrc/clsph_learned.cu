@@ -561,17 +561,24 @@ int ensure_cache(clsph_gpu* h, LearnedCache** out) {
   auto* L = new LearnedCache();
   h->learned = L;
   h->free_learned = free_cache;
+  // a failed allocation leaves no half-made cache behind
+  auto bail = [&](int code) {
+    free_cache(h);
+    return code;
+  };
   const size_t n = h->n;
   int rc;
-  if ((rc = dev_alloc(&L->x, n * kFeat)) || (rc = dev_alloc(&L->corr, n)) || (rc = dev_alloc(&L->dev_sum, kGateSums + 1)))
-    return rc;
-  CUDA_TRY(cudaMemset(L->dev_sum, 0, (kGateSums + 1) * sizeof(float)));
+  if ((rc = dev_alloc(&L->x, n * kFeat)) || (rc = dev_alloc(&L->corr, n)) ||
+      (rc = dev_alloc(&L->dev_sum, kGateSums + 1)))
+    return bail(rc);
   for (auto& s : L->snap)
     if ((rc = dev_alloc(&s.pos, n)) || (rc = dev_alloc(&s.vel, n)) || (rc = dev_alloc(&s.ivel, n)) ||
         (rc = dev_alloc(&s.ids, n)) || (rc = dev_alloc(&s.bbox, 6 * (size_t)h->nscenes)))
-      return rc;
-  CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), (kGateSums + 1) * sizeof(float)));
-  CUDA_TRY(cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming));
+      return bail(rc);
+  if (cudaMemset(L->dev_sum, 0, (kGateSums + 1) * sizeof(float)) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), (kGateSums + 1) * sizeof(float)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(fail(CLSPH_ERR_CUDA, "step_learned: buffer set-up"));
   *out = L;
   return 0;
 }
