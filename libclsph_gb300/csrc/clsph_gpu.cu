@@ -108,7 +108,7 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
       h->launch(K_DENSITY, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
                 (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
-                h->ncount, h->nlist_cap);
+                h->ncount, h->nlist_cap, (const float4*)h->st[1].vel, h->frec);
     };
     if (b == 64) args(k_density<64>);
     else if (b == 256) args(k_density<256>);
@@ -122,7 +122,7 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
       h->launch(K_FORCES, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
                 (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-                (const uint32_t*)h->ncount, h->nlist_cap, h->acc, NoForceHook{});
+                (const uint32_t*)h->ncount, h->nlist_cap, h->acc, NoForceHook{}, (const float4*)h->frec);
     };
     if (b == 64) args(k_forces<64>);
     else if (b == 256) args(k_forces<256>);
@@ -349,7 +349,7 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
   h->slots = slots;
   uint32_t log2s = 0;
   while ((1u << log2s) < slots) ++log2s;
-  if ((rc = dev_alloc(&h->aux, n)) || (rc = dev_alloc(&h->acc, n)) ||
+  if ((rc = dev_alloc(&h->aux, n)) || (rc = dev_alloc(&h->acc, n)) || (rc = dev_alloc(&h->frec, 2 * (size_t)n)) ||
       (rc = dev_alloc(&h->nlist, (size_t)h->nlist_cap * n)) || (rc = dev_alloc(&h->ncount, n)) ||
       (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
       (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
@@ -415,7 +415,7 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->st[s].ivel);
     cudaFree(h->ids[s]);
   }
-  void* bufs[] = {h->aux,      h->acc,      h->nlist,     h->ncount,      h->cell_list,
+  void* bufs[] = {h->aux,      h->acc,      h->frec,      h->nlist,     h->ncount,      h->cell_list,
                   h->step_counters, h->keys, h->vals,     h->tile_hist,   h->digit_total,
                   h->ci.keys,  h->ci.start, h->ci.end,    h->scene_of,    h->grids,
                   h->consts,   h->scene_h,  h->meshes,    h->bbox,        h->ctl,

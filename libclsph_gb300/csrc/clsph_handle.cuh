@@ -125,6 +125,7 @@ struct clsph_gpu {
   int ids_sel = 0;
   float4* aux = nullptr;  // (rho, p, m/rho, p/rho^2)
   float4* acc = nullptr;
+  float4* frec = nullptr;  // [2n] forces records: (pos, m/rho), (vel, p/rho^2)
   uint32_t* nlist = nullptr;
   uint32_t* ncount = nullptr;
   uint32_t nlist_cap = 64;

@@ -690,7 +690,8 @@ __global__ void __launch_bounds__(BLOCK)
               const uint32_t* __restrict__ ctl,
               const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos, CellIndex ci,
               const Consts* __restrict__ consts, float4* __restrict__ aux_out,
-              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap) {
+              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap,
+              const float4* __restrict__ vel, float4* __restrict__ frec) {
   __shared__ uint32_t cand[kScanCap][BLOCK];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -733,7 +734,12 @@ __global__ void __launch_bounds__(BLOCK)
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj);
     });
   }
-  aux_out[i] = density_aux(rho, c);
+  const float4 a = density_aux(rho, c);
+  aux_out[i] = a;
+  // the forces kernel's per-neighbour record: (position, m/rho), (velocity, p/rho^2)
+  const float4 v = vel[i];
+  frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
+  frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
   ncount[i] = kept;  // > nlist_cap: the list is incomplete, forces search again
 }
 
@@ -756,7 +762,7 @@ __global__ void __launch_bounds__(BLOCK)
              const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,
              CellIndex ci, const Consts* __restrict__ consts, const uint32_t* __restrict__ nlist,
              const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
-             float4* __restrict__ acc_out, Hook hook) {
+             float4* __restrict__ acc_out, Hook hook, const float4* __restrict__ frec) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   typename Hook::Acc ha = hook.begin(i);
@@ -769,12 +775,14 @@ __global__ void __launch_bounds__(BLOCK)
   const float hh = XMUL(c.h, c.h);
   const float lap_b = XMUL(3.f, hh);
   ForceSums f = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
+  // neighbour data from the density kernel's 32-byte records
   auto pair = [&](uint32_t j) {
-    const float4 pj = __ldg(&st.pos[j]);
+    const float4 pj = __ldg(&frec[j]);
+    const float4 sj = __ldg(&frec[(size_t)n + j]);
     const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
     const float rr = xnorm(d);
-    const float4 vj = __ldg(&st.vel[j]);
-    force_pair(f, j == i, d, rr, vi, vj, __ldg(&aux[j]), own, hh, lap_b, c);
+    const float4 vj = make_float4(sj.x, sj.y, sj.z, 0.f);
+    force_pair(f, j == i, d, rr, vi, vj, make_float4(0.f, 0.f, pj.w, sj.w), own, hh, lap_b, c);
     hook.pair(ha, i, j, pi, pj, vj);
   };
   const uint32_t cnt = ncount[i];
@@ -785,7 +793,7 @@ __global__ void __launch_bounds__(BLOCK)
     const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
     const Window w = neighbour_window(pi, split.morton(keys[i]), grids[sc]);
     for_each_candidate(w, split.scene_bits(sc), ci, [&](uint32_t j) {
-      const float4 pj = __ldg(&st.pos[j]);
+      const float4 pj = __ldg(&frec[j]);
       const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > c.cull_r2) return;
       const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};

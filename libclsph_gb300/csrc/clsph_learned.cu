@@ -319,7 +319,7 @@ int launch_forces_hooked(clsph_gpu* h, const FeatureHook& hook) {
     h->launch(K_FEATURES, kernel, grid, dim3(b), h->n, (const DevGrid*)h->grids,
               (const uint16_t*)h->scene_of, (const uint32_t*)h->ctl, (const uint32_t*)h->keys, h->st[1],
               (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-              (const uint32_t*)h->ncount, h->nlist_cap, h->acc, hook);
+              (const uint32_t*)h->ncount, h->nlist_cap, h->acc, hook, (const float4*)h->frec);
   };
   if (b == 64) go(k_forces<64, FeatureHook>);
   else if (b == 256) go(k_forces<256, FeatureHook>);
