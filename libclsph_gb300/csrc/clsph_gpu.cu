@@ -110,9 +110,18 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
                 (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
                 h->ncount, h->nlist_cap, (const float4*)h->st[1].vel, h->frec);
     };
-    if (b == 64) args(k_density<64>);
-    else if (b == 256) args(k_density<256>);
-    else args(k_density<128>);
+    if (h->search == CLSPH_SEARCH_CELL_WARPS) {
+      h->launch(K_DENSITY, k_density_cells<kCellWarps>, dim3(h->sm_count * 16), dim3(kCellWarps * 32),
+                n, (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, cctl,
+                (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci,
+                (const Consts*)h->consts, h->aux, h->nlist, h->ncount, h->nlist_cap,
+                (const float4*)h->st[1].vel, h->frec, (const uint32_t*)h->cell_list,
+                h->step_counters);
+    } else {
+      if (b == 64) args(k_density<64>);
+      else if (b == 256) args(k_density<256>);
+      else args(k_density<128>);
+    }
   }
   if (until <= CLSPH_STAGE_DENSITY) return 0;
   {
@@ -164,6 +173,7 @@ int ensure_graph(clsph_gpu* h) {
   const uint64_t launches = h->launches;
   int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
   if (!rc) rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+  h->graph_launches[par] = h->launches - launches;
   h->launches = launches;
   cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
   if (rc) {
@@ -530,7 +540,7 @@ int clsph_gpu_step(clsph_gpu* h, uint32_t substeps) {
     if (rc) return rc;
     for (; done + 2 <= substeps; done += 2) {
       CUDA_TRY(cudaGraphLaunch(h->graph_exec[h->ids_sel], h->stream));
-      h->launches += 2 * kLaunchesPerSubstep;
+      h->launches += h->graph_launches[h->ids_sel];
       h->substeps += 2;
     }
   }
@@ -724,21 +734,27 @@ int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report
   };
   std::string out;
   const int blocks[3] = {64, 128, 256};
-  int best_d = h->density_block, best_f = h->forces_block;
+  const int searches[2] = {CLSPH_SEARCH_WINDOW, CLSPH_SEARCH_CELL_WARPS};
+  int best_d = h->density_block, best_f = h->forces_block, best_s = h->search;
   double td = 1e30, tf = 1e30;
   for (int b : blocks) {
     h->density_block = b;
     h->forces_block = b;
-    trial(K_DENSITY);  // warm-up of this shape
-    double d = trial(K_DENSITY);
+    for (int sm : searches) {
+      h->search = sm;
+      trial(K_DENSITY);  // warm-up of this shape
+      double d = trial(K_DENSITY);
+      out += "density block " + std::to_string(b) + " search " + std::to_string(sm) + ": " +
+             std::to_string(d) + " ms\n";
+      if (d < td) { td = d; best_d = b; best_s = sm; }
+    }
     double f = trial(K_FORCES);
-    out += "density/forces block " + std::to_string(b) + ": " + std::to_string(d) + " / " +
-           std::to_string(f) + " ms\n";
-    if (d < td) { td = d; best_d = b; }
+    out += "forces block " + std::to_string(b) + ": " + std::to_string(f) + " ms\n";
     if (f < tf) { tf = f; best_f = b; }
   }
   h->density_block = best_d;
   h->forces_block = best_f;
+  h->search = best_s;
   const uint32_t advect_opts[3] = {4, 8, 16};
   uint32_t best_a = h->advect_blocks_per_sm;
   double ta = 1e30;
@@ -749,7 +765,8 @@ int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report
     if (t < ta) { ta = t; best_a = a; }
   }
   h->advect_blocks_per_sm = best_a;
-  out += "chosen: density block " + std::to_string(best_d) + ", forces block " + std::to_string(best_f) +
+  out += "chosen: density block " + std::to_string(best_d) + ", search " + std::to_string(best_s) +
+         ", forces block " + std::to_string(best_f) +
          ", advect blocks/SM " + std::to_string(best_a) + "\n";
   h->profiling = prof0;
   for (int k = 0; k < K_NUM_CLASSES; ++k) {
@@ -777,6 +794,16 @@ int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block
   h->density_block = density_block;
   h->forces_block = forces_block;
   h->advect_blocks_per_sm = advect_blocks_per_sm;
+  h->drop_graph();
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_neighbour_search: null handle");
+  if (mode != CLSPH_SEARCH_WINDOW && mode != CLSPH_SEARCH_CELL_WARPS)
+    return fail(CLSPH_ERR_ARGUMENT, "set_neighbour_search: unknown mode");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->search = mode;
   h->drop_graph();
   return CLSPH_OK;
 }

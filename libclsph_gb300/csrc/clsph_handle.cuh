@@ -48,8 +48,6 @@ enum KernelClass {
 
 extern const char* kKernelNames[K_NUM_CLASSES];
 
-// kernels enqueued by one full substep (4 radix passes x 3 kernels)
-constexpr uint32_t kLaunchesPerSubstep = 2 + 12 + 4;
 
 struct PendingTiming {
   int cls;
@@ -144,6 +142,7 @@ struct clsph_gpu {
 
   // launch shapes chosen by clsph_gpu_autotune
   int density_block = 128;
+  int search = CLSPH_SEARCH_CELL_WARPS;  // neighbour search of the density kernel
   int forces_block = 128;
   uint32_t advect_blocks_per_sm = 8;
 
@@ -156,6 +155,7 @@ struct clsph_gpu {
   bool use_graph = false;
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   uint32_t graph_max_iters[2] = {0, 0};
+  uint64_t graph_launches[2] = {0, 0};  // kernels in one replay of each graph
 
   // buffers of the learned stepper (clsph_learned.cu), made on first use
   void* learned = nullptr;

@@ -743,6 +743,151 @@ __global__ void __launch_bounds__(BLOCK)
   ncount[i] = kept;  // > nlist_cap: the list is incomplete, forces search again
 }
 
+// ------------------------------------------------- density, one warp per cell
+// The warp takes one occupied cell at a time (dynamic work counter), looks up
+// the 27 cells around it once (lane k < 27: offset k in the reference's z, y,
+// x loop order) and holds the cell's particles, two per lane. For each
+// neighbour cell, in that order, that lies in at least one particle's window,
+// it stages the cell's candidates that face the own cell (the far half is
+// skipped by half code), 32 at a time and compacted by ballot, which keeps
+// their sorted order, in shared memory. Every lane then tests its particles
+// against the staged candidates (broadcast reads) and appends the survivors to
+// the particle's buffer, so each buffer holds the reference's visiting order.
+// The survivors are then evaluated exactly per particle, as in k_density.
+// A buffer entry is (window cell << 11) | offset in that cell; cells of 2048
+// or more particles and full buffers send the particle to the in-order rescan.
+constexpr int kCellWarps = 4;
+constexpr uint32_t kCellOffBits = 11;
+
+__device__ __forceinline__ bool near_cull(const float4& p, const float4& q, float r2) {
+  const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2;
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_density_cells(uint32_t n, const DevGrid* __restrict__ grids,
+                    const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
+                    const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos,
+                    CellIndex ci, const Consts* __restrict__ consts, float4* __restrict__ aux_out,
+                    uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount,
+                    uint32_t nlist_cap, const float4* __restrict__ vel,
+                    float4* __restrict__ frec, const uint32_t* __restrict__ cell_list,
+                    uint32_t* __restrict__ counters) {
+  __shared__ float4 stage[WARPS][32];
+  __shared__ uint32_t starts[WARPS][32];
+  __shared__ uint16_t cand[WARPS][kScanCap][64];
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t ncells = counters[kCntCells];
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
+  for (;;) {
+    uint32_t cell = 0;
+    if (lane == 0) cell = atomicAdd(&counters[kCntWorkDensity], 1u);
+    cell = __shfl_sync(0xFFFFFFFFu, cell, 0);
+    if (cell >= ncells) break;
+    const uint32_t s0 = cell_list[cell];
+    const uint32_t key = split.morton(keys[s0]);
+    const uint32_t sc = scene_of[s0];
+    const uint32_t sbits = split.scene_bits(sc);
+    const float cull_r2 = consts[sc].cull_r2;
+    const uint32_t cx = compact_bits3(key), cy = compact_bits3(key >> 1), cz = compact_bits3(key >> 2);
+    uint32_t nb_s = 0, nb_e = 0;
+    if (lane < 27u) {
+      const uint32_t x = cx + lane % 3u - 1u, y = cy + (lane / 3u) % 3u - 1u, z = cz + lane / 9u - 1u;
+      const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
+      nb_s = r.x;
+      nb_e = r.y;
+    }
+    starts[wid][lane] = nb_s;
+    __syncwarp();
+    const uint32_t own_e = __shfl_sync(0xFFFFFFFFu, nb_e, 13);
+    const bool wide = __any_sync(0xFFFFFFFFu, nb_e - nb_s >= (1u << kCellOffBits));
+    for (uint32_t base = s0; base < own_e; base += 64u) {
+      const uint32_t ia = base + lane, ib = base + 32u + lane;
+      const bool va = ia < own_e, vb = ib < own_e;
+      const float4 pa = va ? pos[ia] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 pb = vb ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const uint32_t code_a = __float_as_uint(pa.w), code_b = __float_as_uint(pb.w);
+      const bool two = __any_sync(0xFFFFFFFFu, vb);
+      uint32_t fa = wide ? kScanCap + 1u : 0u, fb = fa;
+      for (uint32_t k = 0; k < 27u && !wide; ++k) {
+        const int ox = (int)(k % 3u) - 1, oy = (int)((k / 3u) % 3u) - 1, oz = (int)(k / 9u) - 1;
+        const uint32_t need = facing_mask(-ox, -oy, -oz);  // the own particle's half toward the cell
+        const bool na = va && (code_a & need) == need;
+        const bool nb = vb && (code_b & need) == need;
+        if (!__any_sync(0xFFFFFFFFu, na || nb)) continue;
+        const uint32_t s = __shfl_sync(0xFFFFFFFFu, nb_s, k), e = __shfl_sync(0xFFFFFFFFu, nb_e, k);
+        const uint32_t fm = facing_mask(ox, oy, oz);
+        for (uint32_t cb = s; cb < e; cb += 32u) {
+          const uint32_t j = cb + lane;
+          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+          bool f = false;
+          if (j < e) {
+            q = __ldg(&pos[j]);
+            f = (__float_as_uint(q.w) & fm) == fm;
+          }
+          const uint32_t bal = __ballot_sync(0xFFFFFFFFu, f);
+          if (f) stage[wid][__popc(bal & lt)] = make_float4(q.x, q.y, q.z, __uint_as_float((k << kCellOffBits) | (j - s)));
+          __syncwarp();
+          const uint32_t cnt = __popc(bal);
+          for (uint32_t t = 0; t < cnt; ++t) {
+            const float4 r = stage[wid][t];
+            const uint16_t tag = (uint16_t)__float_as_uint(r.w);
+            if (na && near_cull(pa, r, cull_r2)) {
+              if (fa < (uint32_t)kScanCap) cand[wid][fa][lane] = tag;
+              ++fa;
+            }
+            if (two && nb && near_cull(pb, r, cull_r2)) {
+              if (fb < (uint32_t)kScanCap) cand[wid][fb][lane + 32u] = tag;
+              ++fb;
+            }
+          }
+          __syncwarp();
+        }
+      }
+      auto finish = [&](uint32_t i, const float4& pi, uint32_t found, uint32_t col) {
+        const Consts& c = consts[sc];
+        const float hh = XMUL(c.h, c.h);
+        float rho = 0.f;
+        uint32_t kept = 0;
+        auto visit = [&](uint32_t j, float4 pj) {
+          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+          const float rr = xnorm(d);
+          if (rr < c.h) {
+            rho = XADD(rho, poly6_term(rr, hh, c));
+            if (kept < nlist_cap) nlist[(size_t)kept * n + i] = j;
+            ++kept;
+          }
+        };
+        if (found <= (uint32_t)kScanCap) {
+          for (uint32_t k = 0; k < found; ++k) {
+            const uint32_t tag = cand[wid][k][col];
+            const uint32_t j = starts[wid][tag >> kCellOffBits] + (tag & ((1u << kCellOffBits) - 1u));
+            visit(j, __ldg(&pos[j]));
+          }
+        } else {
+          const Window w = neighbour_window(pi, key, grids[sc]);
+          for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
+            if (near_cull(pi, pj, c.cull_r2)) visit(j, pj);
+          });
+        }
+        const float4 a = density_aux(rho, c);
+        aux_out[i] = a;
+        const float4 v = vel[i];
+        frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
+        frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
+        ncount[i] = kept;
+      };
+      if (va) finish(ia, pa, fa, lane);
+      if (vb) finish(ib, pb, fb, lane + 32u);
+      __syncwarp();
+    }
+    __syncwarp();
+  }
+}
+
 // Per-pair hook of k_forces (the learned stepper gathers its neighbour
 // features in the same walk); the plain substep uses this empty one.
 struct NoForceHook {

@@ -18,6 +18,9 @@ from .layout import PARAMS, PARTICLE, TERMS
 _LIB = None
 
 STAGE_GRID, STAGE_SORT, STAGE_DENSITY, STAGE_FORCES, STAGE_ADVECT = 1, 2, 3, 4, 5
+# neighbour search modes of the density kernel (include/clsph_gpu.h)
+SEARCH_WINDOW, SEARCH_CELL_WARPS = 0, 1
+SEARCH_MODES = (SEARCH_WINDOW, SEARCH_CELL_WARPS)
 WARN_GRID_OVERFLOW, WARN_COLLISION_CAP, WARN_NONFINITE = 1, 2, 4
 
 _vp = ctypes.c_void_p
@@ -52,6 +55,7 @@ SIGNATURES = [
     ("clsph_gpu_sort_keys_noalloc", ctypes.c_int, [_vp, _vp, _vp, _u32, _vp]),
     ("clsph_gpu_autotune", ctypes.c_int, [_vp, _u32, ctypes.c_char_p, ctypes.c_int]),
     ("clsph_gpu_set_launch_shape", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u32]),
+    ("clsph_gpu_set_neighbour_search", ctypes.c_int, [_vp, ctypes.c_int]),
     ("clsph_gpu_last_error", ctypes.c_char_p, []),
 ]
 
@@ -268,6 +272,10 @@ class GpuSolver:
         _check("clsph_gpu_set_launch_shape",
                self.lib.clsph_gpu_set_launch_shape(self.h, density_block, forces_block,
                                                    advect_blocks_per_sm))
+
+    def set_neighbour_search(self, mode: int) -> None:
+        """SEARCH_WINDOW or SEARCH_CELL_WARPS (bit-identical results, different speed)."""
+        _check("clsph_gpu_set_neighbour_search", self.lib.clsph_gpu_set_neighbour_search(self.h, mode))
 
     def counters(self) -> dict:
         c = np.zeros(3, dtype=np.uint64)
