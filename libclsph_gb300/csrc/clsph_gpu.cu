@@ -110,13 +110,16 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
                 (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
                 h->ncount, h->nlist_cap, (const float4*)h->st[1].vel, h->frec);
     };
-    if (h->search == CLSPH_SEARCH_CELL_WARPS) {
-      h->launch(K_DENSITY, k_density_cells<kCellWarps>, dim3(h->sm_count * 16), dim3(kCellWarps * 32),
+    auto cells = [&](auto kernel) {
+      h->launch(K_DENSITY, kernel, dim3(h->sm_count * 16), dim3(kCellWarps * 32),
                 n, (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, cctl,
                 (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci,
                 (const Consts*)h->consts, h->aux, h->nlist, h->ncount, h->nlist_cap,
                 (const float4*)h->st[1].vel, h->frec, (const uint32_t*)h->cell_list,
                 h->step_counters);
+    };
+    if (h->search == CLSPH_SEARCH_CELL_WARPS) {
+      cells(k_density_cells<kCellWarps>);
     } else {
       if (b == 64) args(k_density<64>);
       else if (b == 256) args(k_density<256>);
