@@ -553,7 +553,9 @@ static __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
 // Per particle the density kernel also stores (rho, p, m/rho, p/rho^2) -- the
 // same IEEE quotients the reference forms per pair -- and the list of its
 // contributing neighbours in visiting order (column-major, nlist[k*n + i]),
-// which the forces kernel walks without a second search.
+// which the forces kernel walks without a second search. The list is stored
+// and read with evict-first (streaming) hints: it is read once, and at 1M
+// particles it is larger than L2, where the neighbour records should stay.
 
 constexpr int kGatherBlock = 128;
 
@@ -719,7 +721,7 @@ __global__ void __launch_bounds__(BLOCK)
     const float rr = xnorm(d);
     if (rr < c.h) {
       rho = XADD(rho, poly6_term(rr, hh, c));
-      if (kept < nlist_cap) nlist[(size_t)kept * n + i] = j;
+      if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], j);
       ++kept;
     }
   };
@@ -865,7 +867,7 @@ __global__ void __launch_bounds__(WARPS * 32)
           const float rr = xnorm(d);
           if (rr < c.h) {
             rho = XADD(rho, poly6_term(rr, hh, c));
-            if (kept < nlist_cap) nlist[(size_t)kept * n + i] = j;
+            if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], j);
             ++kept;
           }
         };
@@ -943,11 +945,11 @@ __global__ void __launch_bounds__(BLOCK)
     // software pipeline: the list entry two pairs ahead and the records of
     // the next pair are in flight while a pair is evaluated
     if (cnt > 0) {
-      uint32_t j = __ldg(&nlist[i]);
-      uint32_t jn = cnt > 1 ? __ldg(&nlist[(size_t)n + i]) : j;
+      uint32_t j = __ldcs(&nlist[i]);
+      uint32_t jn = cnt > 1 ? __ldcs(&nlist[(size_t)n + i]) : j;
       float4 pj = __ldg(&frec[j]), sj = __ldg(&frec[(size_t)n + j]);
       for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t jnn = k + 2 < cnt ? __ldg(&nlist[(size_t)(k + 2) * n + i]) : jn;
+        const uint32_t jnn = k + 2 < cnt ? __ldcs(&nlist[(size_t)(k + 2) * n + i]) : jn;
         const float4 pn = __ldg(&frec[jn]), sn = __ldg(&frec[(size_t)n + jn]);
         pair_with(j, pj, sj);
         j = jn;
