@@ -182,7 +182,7 @@ int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_
                            float* ms, uint32_t* counts, int* n_classes);
 
 /* Autotuner (no counterpart in the reference): times the density kernel in
- * both neighbour search modes and the density and forces kernels at
+ * every neighbour search mode and the density and forces kernels at
  * 64/128/256 threads per block, and the
  * advection grid at 4/8/16 blocks per SM, `substeps` substeps per trial, on
  * the handle's current
@@ -197,15 +197,18 @@ int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block
                                uint32_t advect_blocks_per_sm);
 
 /* Neighbour search of the density kernel (no counterpart in the reference;
- * both modes give bit-identical results, they differ only in speed):
+ * all modes give bit-identical results, they differ only in speed):
  *  WINDOW: one thread per particle walks its 2x2x2 window of cells and skips
  *    the particles in each neighbour cell's far half by their half-cell code;
  *  CELL_WARPS: one warp per occupied cell stages each neighbour cell's facing
- *    half in shared memory once for all of the cell's particles. The default.
+ *    half in shared memory once for all of the cell's particles. The default;
+ *  PARTICLE_WARPS: one warp per particle tests 32 candidates at a time (for
+ *    scenes too small to fill the GPU otherwise).
  * The block size of clsph_gpu_set_launch_shape applies to WINDOW only. */
 enum {
   CLSPH_SEARCH_WINDOW = 0,
-  CLSPH_SEARCH_CELL_WARPS = 1
+  CLSPH_SEARCH_CELL_WARPS = 1,
+  CLSPH_SEARCH_PARTICLE_WARPS = 2
 };
 int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode);
 

@@ -120,6 +120,12 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
     };
     if (h->search == CLSPH_SEARCH_CELL_WARPS) {
       cells(k_density_cells<kCellWarps>);
+    } else if (h->search == CLSPH_SEARCH_PARTICLE_WARPS) {
+      h->launch(K_DENSITY, k_density_pwarp, dim3((n + kParticleWarps - 1) / kParticleWarps),
+                dim3(kParticleWarps * 32), n, (const DevGrid*)h->grids, (const uint16_t*)h->scene_of,
+                cctl, (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci,
+                (const Consts*)h->consts, h->aux, h->nlist, h->ncount, h->nlist_cap,
+                (const float4*)h->st[1].vel, h->frec);
     } else {
       if (b == 64) args(k_density<64>);
       else if (b == 256) args(k_density<256>);
@@ -737,7 +743,7 @@ int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report
   };
   std::string out;
   const int blocks[3] = {64, 128, 256};
-  const int searches[2] = {CLSPH_SEARCH_WINDOW, CLSPH_SEARCH_CELL_WARPS};
+  const int searches[3] = {CLSPH_SEARCH_WINDOW, CLSPH_SEARCH_CELL_WARPS, CLSPH_SEARCH_PARTICLE_WARPS};
   int best_d = h->density_block, best_f = h->forces_block, best_s = h->search;
   double td = 1e30, tf = 1e30;
   for (int b : blocks) {
@@ -803,7 +809,7 @@ int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block
 
 int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode) {
   if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_neighbour_search: null handle");
-  if (mode != CLSPH_SEARCH_WINDOW && mode != CLSPH_SEARCH_CELL_WARPS)
+  if (mode != CLSPH_SEARCH_WINDOW && mode != CLSPH_SEARCH_CELL_WARPS && mode != CLSPH_SEARCH_PARTICLE_WARPS)
     return fail(CLSPH_ERR_ARGUMENT, "set_neighbour_search: unknown mode");
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   h->search = mode;

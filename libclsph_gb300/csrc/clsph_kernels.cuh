@@ -899,6 +899,81 @@ __global__ void __launch_bounds__(WARPS * 32)
 }
 
 
+// Density + pressure + neighbour list with one warp per particle, for scenes
+// too small to fill the GPU with one thread per particle or one warp per
+// cell. The warp walks the particle's window cells in the reference's order,
+// 32 candidates at a time (far halves skipped by half code, FMA cull), every
+// lane evaluates its candidate exactly, and the contributing terms are added
+// to the density one after another in lane order (ballot + shuffle), which is
+// the reference's visiting order; survivors append to the neighbour list in
+// the same order.
+constexpr int kParticleWarps = 8;
+
+static __global__ void __launch_bounds__(kParticleWarps * 32)
+    k_density_pwarp(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+                    const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ keys_base,
+                    const float4* __restrict__ pos, CellIndex ci, const Consts* __restrict__ consts,
+                    float4* __restrict__ aux_out, uint32_t* __restrict__ nlist,
+                    uint32_t* __restrict__ ncount, uint32_t nlist_cap, const float4* __restrict__ vel,
+                    float4* __restrict__ frec) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= n) return;  // whole warps
+  const KeySplit split{ctl[kCtlShift]};
+  const uint32_t sc = scene_of[i];
+  const Consts& c = consts[sc];
+  const uint32_t sbits = split.scene_bits(sc);
+  const uint32_t* keys = keys_base + (size_t)sorted_sel(ctl[kCtlMaxKey]) * n;
+  const uint32_t key = split.morton(keys[i]);
+  const float4 pi = pos[i];
+  const Window w = neighbour_window(pi, key, grids[sc]);
+  const int cc[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
+  const float hh = XMUL(c.h, c.h);
+  const float h = c.h, cull_r2 = c.cull_r2;
+  float rho = 0.f;
+  uint32_t kept = 0;
+  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
+    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
+      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
+        const uint32_t need = facing_mask((int)x - cc[0], (int)y - cc[1], (int)z - cc[2]);
+        const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
+        for (uint32_t cb = r.x; cb < r.y; cb += 32u) {
+          const uint32_t j = cb + lane;
+          bool hit = false;
+          float term = 0.f;
+          if (j < r.y) {
+            const float4 pj = __ldg(&pos[j]);
+            if ((__float_as_uint(pj.w) & need) == need && near_cull(pi, pj, cull_r2)) {
+              const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+              const float rr = xnorm(d);
+              if (rr < h) {
+                hit = true;
+                term = poly6_term(rr, hh, c);
+              }
+            }
+          }
+          uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+          const uint32_t at = kept + __popc(bal & lt);
+          if (hit && at < nlist_cap) __stcs(&nlist[(size_t)at * n + i], j);
+          kept += __popc(bal);
+          while (bal) {  // in lane order: the reference's summation sequence
+            const int l = __ffs(bal) - 1;
+            rho = XADD(rho, __shfl_sync(0xFFFFFFFFu, term, l));
+            bal &= bal - 1u;
+          }
+        }
+      }
+  if (lane == 0) {
+    const float4 a = density_aux(rho, c);
+    aux_out[i] = a;
+    const float4 v = vel[i];
+    frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
+    frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
+    ncount[i] = kept;
+  }
+}
+
 // Per-pair hook of k_forces (the learned stepper gathers its neighbour
 // features in the same walk); the plain substep uses this empty one.
 struct NoForceHook {

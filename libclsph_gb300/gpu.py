@@ -19,8 +19,8 @@ _LIB = None
 
 STAGE_GRID, STAGE_SORT, STAGE_DENSITY, STAGE_FORCES, STAGE_ADVECT = 1, 2, 3, 4, 5
 # neighbour search modes of the density kernel (include/clsph_gpu.h)
-SEARCH_WINDOW, SEARCH_CELL_WARPS = 0, 1
-SEARCH_MODES = (SEARCH_WINDOW, SEARCH_CELL_WARPS)
+SEARCH_WINDOW, SEARCH_CELL_WARPS, SEARCH_PARTICLE_WARPS = 0, 1, 2
+SEARCH_MODES = (SEARCH_WINDOW, SEARCH_CELL_WARPS, SEARCH_PARTICLE_WARPS)
 WARN_GRID_OVERFLOW, WARN_COLLISION_CAP, WARN_NONFINITE = 1, 2, 4
 
 _vp = ctypes.c_void_p
@@ -274,7 +274,7 @@ class GpuSolver:
                                                    advect_blocks_per_sm))
 
     def set_neighbour_search(self, mode: int) -> None:
-        """SEARCH_WINDOW or SEARCH_CELL_WARPS (bit-identical results, different speed)."""
+        """SEARCH_WINDOW, SEARCH_CELL_WARPS or SEARCH_PARTICLE_WARPS (bit-identical results)."""
         _check("clsph_gpu_set_neighbour_search", self.lib.clsph_gpu_set_neighbour_search(self.h, mode))
 
     def counters(self) -> dict:
