@@ -1130,8 +1130,10 @@ __device__ __forceinline__ bool nearest_hit(const DevMesh& m, V3 p0, V3 p1, Hit&
 // advance with (1 - pos_w) v + pos_w v' instead of v' (pos_w = (m + 1) / 2m
 // for m = dt_mult reproduces m leapfrog substeps exactly under constant
 // acceleration; m = 1 is the plain update).
+// (4 resident blocks of 256 threads: 64 registers, against 90 and 2 blocks
+// unconstrained; 23 % faster on the 1M dam break)
 template <bool kLearned>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
     k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out,
              const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
              const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
