@@ -506,36 +506,58 @@ static __global__ void __launch_bounds__(kRadixThreads)
 // Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
 // and records every cell's [start, end) in the cell index (the dense cell
 // table of sph_simulation.cpp:162-170 in compact form).
-static __global__ void k_gather(uint32_t n, const DevGrid* __restrict__ grids,
-                         const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
-                         const uint32_t* __restrict__ keys_base,
-                         const uint32_t* __restrict__ vals_base, State src, State dst,
-                         const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
-                         CellIndex ci, uint32_t* __restrict__ cell_list,
-                         uint32_t* __restrict__ cell_count) {
+// Cell starts join the cell list with one atomic per block (slot order is
+// kept within the block, so the list stays close to sorted order).
+static __global__ void __launch_bounds__(kBlock)
+    k_gather(uint32_t n, const DevGrid* __restrict__ grids,
+             const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
+             const uint32_t* __restrict__ keys_base,
+             const uint32_t* __restrict__ vals_base, State src, State dst,
+             const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
+             CellIndex ci, uint32_t* __restrict__ cell_list,
+             uint32_t* __restrict__ cell_count) {
+  __shared__ uint32_t warp_base[kBlock / 32];
+  __shared__ uint32_t block_base;
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const KeySplit split{ctl[kCtlShift]};
   const uint32_t sel = sorted_sel(ctl[kCtlMaxKey]);
   const uint32_t* keys = keys_base + (size_t)sel * n;
   const uint32_t* perm = vals_base + (size_t)sel * n;
-  const uint32_t from = perm[s];
-  const uint32_t key = keys[s];
-  float4 p = src.pos[from];
-  p.w = __uint_as_float(half_code(p, split.morton(key), grids[scene_of[s]]));
-  dst.pos[s] = p;
-  dst.vel[s] = src.vel[from];
-  dst.ivel[s] = src.ivel[from];
-  ids_dst[s] = ids_src[from];
-  if (s == 0 || keys[s - 1] != key) {
-    uint32_t slot = cell_slot_insert(ci, key);
-    if (slot != 0xFFFFFFFFu) ci.start[slot] = s;
-    cell_list[atomicAdd(cell_count, 1u)] = s;
+  bool first = false;
+  if (s < n) {
+    const uint32_t from = perm[s];
+    const uint32_t key = keys[s];
+    float4 p = src.pos[from];
+    p.w = __uint_as_float(half_code(p, split.morton(key), grids[scene_of[s]]));
+    dst.pos[s] = p;
+    dst.vel[s] = src.vel[from];
+    dst.ivel[s] = src.ivel[from];
+    ids_dst[s] = ids_src[from];
+    first = s == 0 || keys[s - 1] != key;
+    if (first) {
+      uint32_t slot = cell_slot_insert(ci, key);
+      if (slot != 0xFFFFFFFFu) ci.start[slot] = s;
+    }
+    if (s + 1 == n || keys[s + 1] != key) {
+      uint32_t slot = cell_slot_insert(ci, key);
+      if (slot != 0xFFFFFFFFu) ci.end[slot] = s + 1;
+    }
   }
-  if (s + 1 == n || keys[s + 1] != key) {
-    uint32_t slot = cell_slot_insert(ci, key);
-    if (slot != 0xFFFFFFFFu) ci.end[slot] = s + 1;
+  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, first);
+  if (lane == 0) warp_base[warp] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int w = 0; w < kBlock / 32; ++w) {
+      const uint32_t c = warp_base[w];
+      warp_base[w] = run;
+      run += c;
+    }
+    block_base = run ? atomicAdd(cell_count, run) : 0u;
   }
+  __syncthreads();
+  if (first) cell_list[block_base + warp_base[warp] + __popc(bal & ((1u << lane) - 1u))] = s;
 }
 
 // ------------------------------------------------- density and forces
