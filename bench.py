@@ -528,8 +528,11 @@ def main() -> None:
             "h_m": scene.info.get("h"),
             "scenes": scene.info.get("scenes", 1),
             "faces": len(scene.mesh["indices"]) // 3,
-            "l2": "256 MiB buffer written before every timed step, outside the step's events"
-                  if not args.no_flush else "no flush",
+            "l2": ("inputs larger than L2: a substep moves about 600 B per particle through DRAM "
+                   "(neighbour lists, records, state; profiles/dram_bytes_per_particle.json); in addition "
+                   f"a 256 MiB buffer is written before every timed launch of {unit} substep(s), outside "
+                   "the events") if not args.no_flush else
+                  "inputs larger than L2: a substep moves about 600 B per particle through DRAM; no flush",
             "sim_s_per_s": value / n * float(scene.params["time_delta"] * scene.params["simulation_scale"]),
             "wall_s_timed_region": wall,
         },
