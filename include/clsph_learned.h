@@ -19,8 +19,8 @@
  *     of the step, max(|D - D_pred|, |M - M_pred|) over the particles with
  *     D = mean |rho/rho0 - 1| and M = mean rho/rho0 of the densities reached
  *     (rho) and predicted (rho_pred); above the threshold the step is rolled
- *     back and replaced by dt_mult plain substeps (the plain solver is the
- *     fallback and the judge).
+ *     back and replaced by dt_mult plain substeps (the plain solver is both
+ *     the fallback and the standard the step is measured against).
  *
  * Features of particle i (h, dt = time_delta * simulation_scale, rho0, K and
  * vmax of its scene; sums over contributing neighbours j != i,

@@ -7,13 +7,13 @@ substep: the 32 neighbour features at substep t and the correction that
 makes one 4 dt step from t land on the velocity 4 plain substeps reach, plus
 the density change over those substeps.
 
-Round 1 samples the plain trajectories and trains the network. An optional
-round 2 (--learned-steps > 0) runs that network's learned steps from the
+Stage 1 samples the plain trajectories and trains the network. An optional
+stage 2 (--learned-steps > 0) runs that network's learned steps from the
 same start, samples the plain outcome of every state they visit (the states
 a learned stepper actually reaches) and trains the final network on both
 sets; on the large dam break it did not lower the density deviation of
 learned runs, so it is off by default. The last `--holdout` fraction of each
-round's substeps is kept for validation. Everything runs through the
+stage's substeps is kept for validation. Everything runs through the
 engine's own kernels (include/clsph_learned.h); torch is not used.
 
     python -m libclsph_gb300.train_stepper [--substeps 1000] [--learned-steps 0]
@@ -85,7 +85,7 @@ def main(argv=None) -> dict:
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--substeps", type=int, default=1000)
     ap.add_argument("--learned-steps", type=int, default=0,
-                    help="second round: learned steps of the first network whose visited states are sampled")
+                    help="second stage: learned steps of the first network whose visited states are sampled")
     ap.add_argument("--stride", type=int, default=64)
     ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--batch", type=int, default=65536)
@@ -111,29 +111,29 @@ def main(argv=None) -> dict:
     val1 = m * max(1, int(round(n1 // m * args.holdout)))
     t_collect = time.perf_counter() - t0
 
-    # round 1: the plain trajectories
+    # stage 1: the plain trajectories
     mlp1, n_train1, t_train1, log1 = train_on(col, 0, n1 - val1, args, args.seed)
     report = {
         "scenes": args.scenes, "particles": int(solver.n), "substeps": args.substeps,
         "tracked_per_substep": m, "epochs": args.epochs, "batch": args.batch, "lr": args.lr,
         "lr_final": args.lr_final, "collect_s": t_collect,
-        "round1": {"samples": int(n1), "train_samples": int(n_train1), "val_samples": int(val1),
+        "stage1": {"samples": int(n1), "train_samples": int(n_train1), "val_samples": int(val1),
                    "train_s": t_train1, "val_outputs": output_quality(mlp1, col, n1 - val1, val1),
                    "loss_log": [float(v) for v in log1]},
     }
     final = mlp1
     if args.learned_steps:
-        # round 2: the states the first network's learned steps reach, from the start
+        # stage 2: the states the first network's learned steps reach, from the start
         t1 = time.perf_counter()
         solver.upload(initial)
         flags |= collect_learned(solver, col, mlp1, args.learned_steps)
         n2 = col.samples()[2]
         val2 = m * max(1, int(round((n2 - n1) // m * args.holdout)))
         mlp2, n_train2, t_train2, log2 = train_on(col, 0, n2 - val2, args, args.seed + 1)
-        report["round2"] = {"samples": int(n2 - n1), "collect_s": time.perf_counter() - t1 - t_train2,
+        report["stage2"] = {"samples": int(n2 - n1), "collect_s": time.perf_counter() - t1 - t_train2,
                             "train_samples": int(n_train2), "val_samples": int(val2), "train_s": t_train2,
                             "val_outputs": output_quality(mlp2, col, n2 - val2, val2),
-                            "val_outputs_round1_net": output_quality(mlp1, col, n2 - val2, val2),
+                            "val_outputs_stage1_net": output_quality(mlp1, col, n2 - val2, val2),
                             "loss_log": [float(v) for v in log2]}
         final = mlp2
         mlp1.close()
@@ -147,8 +147,8 @@ def main(argv=None) -> dict:
     col.close()
     solver.close()
     final.close()
-    brief = {k: v for k, v in report.items() if not k.startswith("round")}
-    for r in ("round1", "round2"):
+    brief = {k: v for k, v in report.items() if not k.startswith("stage")}
+    for r in ("stage1", "stage2"):
         if r in report:
             brief[r] = {k: v for k, v in report[r].items() if k != "loss_log"}
     print(json.dumps(brief))
