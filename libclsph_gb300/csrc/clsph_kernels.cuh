@@ -395,10 +395,22 @@ static __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uin
   const uint32_t* keys = keys_base + (size_t)(pass & 1) * n;
   const uint32_t base = blockIdx.x * kRadixTile;
   const int shift = 8 * pass;
-#pragma unroll 4
-  for (int k = 0; k < kRadixItems; ++k) {
-    uint32_t idx = base + k * kRadixThreads + threadIdx.x;
-    if (idx < n) atomicAdd(&hist[(__ldg(&keys[idx]) >> shift) & 0xFFu], 1u);
+  // the order of counting does not matter: 16-byte loads, 4 keys each
+  // (scalar loads at the end of the keys and where the second ping-pong
+  // buffer, n keys in, is not 16-byte aligned)
+  static_assert(kRadixItems % 4 == 0, "vector loads of the count kernel");
+#pragma unroll
+  for (int k = 0; k < kRadixItems / 4; ++k) {
+    const uint32_t idx = base + (k * kRadixThreads + threadIdx.x) * 4u;
+    if (idx + 3u < n && (reinterpret_cast<uintptr_t>(keys + idx) & 15u) == 0u) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4*>(keys + idx));
+      atomicAdd(&hist[(q.x >> shift) & 0xFFu], 1u);
+      atomicAdd(&hist[(q.y >> shift) & 0xFFu], 1u);
+      atomicAdd(&hist[(q.z >> shift) & 0xFFu], 1u);
+      atomicAdd(&hist[(q.w >> shift) & 0xFFu], 1u);
+    } else {
+      for (uint32_t e = idx; e < idx + 4u && e < n; ++e) atomicAdd(&hist[(__ldg(&keys[e]) >> shift) & 0xFFu], 1u);
+    }
   }
   __syncthreads();
   uint32_t c = hist[threadIdx.x];
