@@ -969,37 +969,51 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
   const float h = c.h, cull_r2 = c.cull_r2;
   float rho = 0.f;
   uint32_t kept = 0;
-  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
-    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
-      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
-        const uint32_t need = facing_mask((int)x - cc[0], (int)y - cc[1], (int)z - cc[2]);
-        const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
-        for (uint32_t cb = r.x; cb < r.y; cb += 32u) {
-          const uint32_t j = cb + lane;
-          bool hit = false;
-          float term = 0.f;
-          if (j < r.y) {
-            const float4 pj = __ldg(&pos[j]);
-            if ((__float_as_uint(pj.w) & need) == need && near_cull(pi, pj, cull_r2)) {
-              const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
-              const float rr = xnorm(d);
-              if (rr < h) {
-                hit = true;
-                term = poly6_term(rr, hh, c);
-              }
-            }
-          }
-          uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
-          const uint32_t at = kept + __popc(bal & lt);
-          if (hit && at < nlist_cap) __stcs(&nlist[(size_t)at * n + i], j);
-          kept += __popc(bal);
-          while (bal) {  // in lane order: the reference's summation sequence
-            const int l = __ffs(bal) - 1;
-            rho = XADD(rho, __shfl_sync(0xFFFFFFFFu, term, l));
-            bal &= bal - 1u;
+  // lane k < 27 looks up window cell k (z, y, x order) in parallel
+  uint32_t cs = 0, ce = 0;
+  bool inw = false;
+  if (lane < 27u) {
+    const uint32_t x = (uint32_t)cc[0] + lane % 3u - 1u, y = (uint32_t)cc[1] + (lane / 3u) % 3u - 1u,
+                   z = (uint32_t)cc[2] + lane / 9u - 1u;
+    inw = x >= w.lo[0] && x <= w.hi[0] && y >= w.lo[1] && y <= w.hi[1] && z >= w.lo[2] && z <= w.hi[2];
+    if (inw) {
+      const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
+      cs = r.x;
+      ce = r.y;
+    }
+  }
+  uint32_t cells = __ballot_sync(0xFFFFFFFFu, inw && ce > cs);
+  while (cells) {
+    const uint32_t k = __ffs(cells) - 1u;
+    cells &= cells - 1u;
+    const uint32_t need = facing_mask((int)(k % 3u) - 1, (int)((k / 3u) % 3u) - 1, (int)(k / 9u) - 1);
+    const uint2 r = make_uint2(__shfl_sync(0xFFFFFFFFu, cs, k), __shfl_sync(0xFFFFFFFFu, ce, k));
+    for (uint32_t cb = r.x; cb < r.y; cb += 32u) {
+      const uint32_t j = cb + lane;
+      bool hit = false;
+      float term = 0.f;
+      if (j < r.y) {
+        const float4 pj = __ldg(&pos[j]);
+        if ((__float_as_uint(pj.w) & need) == need && near_cull(pi, pj, cull_r2)) {
+          const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
+          const float rr = xnorm(d);
+          if (rr < h) {
+            hit = true;
+            term = poly6_term(rr, hh, c);
           }
         }
       }
+      uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+      const uint32_t at = kept + __popc(bal & lt);
+      if (hit && at < nlist_cap) __stcs(&nlist[(size_t)at * n + i], j);
+      kept += __popc(bal);
+      while (bal) {  // in lane order: the reference's summation sequence
+        const int l = __ffs(bal) - 1;
+        rho = XADD(rho, __shfl_sync(0xFFFFFFFFu, term, l));
+        bal &= bal - 1u;
+      }
+    }
+  }
   if (lane == 0) {
     const float4 a = density_aux(rho, c);
     aux_out[i] = a;
