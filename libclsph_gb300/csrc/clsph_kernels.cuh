@@ -794,9 +794,10 @@ __global__ void __launch_bounds__(BLOCK)
 // The survivors are then evaluated exactly per particle, as in k_density.
 // A buffer entry is (window cell << 11) | offset in that cell; cells of 2048
 // or more particles and full buffers send the particle to the in-order rescan.
-// (Register use matters more than occupancy here: capping the kernel at 56
-// registers for 8 resident blocks made it 25 % slower, and a half2 staging
-// cull that tests both of a lane's particles per instruction gained nothing.)
+// This form runs at 64 registers and 27 KB of shared memory per block of 4
+// warps, 8 resident blocks per SM; variants that needed more registers (a
+// packed f32x2 or TF32 tensor-core cull, 64-slot chunks, x-half slot pairs)
+// or forced fewer (a 56-register cap) measured slower.
 constexpr int kCellWarps = 4;
 constexpr uint32_t kCellOffBits = 11;
 
