@@ -88,9 +88,11 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   if (until <= CLSPH_STAGE_GRID) return 0;
   for (int pass = 0; pass < 4; ++pass) {
     h->launch(K_RADIX_COUNT, k_radix_count, dim3(h->ntiles), dim3(kRadixThreads),
-              (const uint32_t*)h->keys, n, pass, cctl, h->tile_hist, h->ntiles, h->digit_total);
-    h->launch(K_RADIX_SCAN, k_radix_scan, dim3(256), dim3(kRadixThreads), h->tile_hist, h->ntiles,
-              pass, cctl, (const uint32_t*)h->digit_total);
+              (const uint32_t*)h->keys, n, pass, cctl, h->tile_hist, h->ntiles, h->digit_total,
+              h->step_counters + kCntRadixTicket);
+    if (h->ntiles > kRadixFuseScanTiles)
+      h->launch(K_RADIX_SCAN, k_radix_scan, dim3(256), dim3(kRadixThreads), h->tile_hist, h->ntiles,
+                pass, cctl, (const uint32_t*)h->digit_total);
     h->launch(K_RADIX_SCATTER, k_radix_scatter, dim3(h->ntiles), dim3(kRadixThreads), h->keys,
               h->vals, n, pass, cctl, (const uint32_t*)h->tile_hist, h->ntiles);
   }

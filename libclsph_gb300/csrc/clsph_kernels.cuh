@@ -33,7 +33,7 @@ constexpr int kRadixWarpSpan = kRadixTile / kRadixWarps;  // 256 keys per warp
 
 // per-substep counters, zeroed by k_grid_setup
 constexpr int kStepCounters = 8;
-enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntWorkForces = 2 };
+enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntWorkForces = 2, kCntRadixTicket = 3 };
 
 enum : uint32_t {
   kFlagGridOverflow = 1u,
@@ -385,11 +385,18 @@ static __global__ void __launch_bounds__(kBlock)
 // scatter per pass. Passes beyond DevGrid::passes return at once, so the
 // launch sequence is fixed (graph-capturable) while the work follows the
 // key width. Ping-pong: pass p reads buffer p&1 and writes (p+1)&1.
+// Tiles at or below which the last count block scans the per-tile counts
+// itself (small scenes: the separate scan launch is mostly latency).
+constexpr uint32_t kRadixFuseScanTiles = 64;
+
 static __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
                               const uint32_t* __restrict__ ctl, uint32_t* __restrict__ tile_hist,
-                              uint32_t ntiles, uint32_t* __restrict__ digit_total) {
+                              uint32_t ntiles, uint32_t* __restrict__ digit_total,
+                              uint32_t* __restrict__ ticket) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t hist[256];
+  __shared__ uint32_t warp_sums[256 / 32];
+  __shared__ bool last;
   hist[threadIdx.x] = 0u;
   __syncthreads();
   const uint32_t* keys = keys_base + (size_t)(pass & 1) * n;
@@ -416,6 +423,34 @@ static __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uin
   uint32_t c = hist[threadIdx.x];
   tile_hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
   if (c) atomicAdd(&digit_total[pass * 256 + threadIdx.x], c);
+  if (ntiles > kRadixFuseScanTiles) return;
+  // small scenes: the last block to finish turns the counts into offsets
+  // (what k_radix_scan does), so the scan needs no launch of its own
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1u;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const uint32_t d = threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t tot = __ldcg(&digit_total[pass * 256 + d]);
+  uint32_t x = tot;  // inclusive scan over the 256 digits
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  uint32_t run = x - tot;
+  for (int w = 0; w < warp; ++w) run += warp_sums[w];
+  uint32_t* row = tile_hist + (size_t)d * ntiles;
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    const uint32_t v = __ldcg(&row[t]);
+    row[t] = run;
+    run += v;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;  // for the next pass
 }
 
 // One block per digit: exclusive scan of that digit's per-tile counts plus
