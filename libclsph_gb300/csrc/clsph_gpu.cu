@@ -171,20 +171,22 @@ int clsph_host::check_launch(clsph_gpu* h) {
 
 namespace {
 
-// Two substeps captured once and replayed. The particle ids alternate between
-// their two buffers, so a pair returns them to the buffer it started from;
-// there is one graph per starting buffer.
-int ensure_graph(clsph_gpu* h) {
+// An even number of substeps (kGraphLen[kind]) captured once and replayed.
+// The particle ids alternate between their two buffers, so an even count
+// returns them to the buffer it started from; there is one graph per
+// starting buffer.
+int ensure_graph(clsph_gpu* h, int kind) {
   const int par = h->ids_sel;
-  if (h->graph_exec[par] && h->graph_max_iters[par] == h->max_iters) return 0;
-  if (h->graph_exec[par]) cudaGraphExecDestroy(h->graph_exec[par]);
-  h->graph_exec[par] = nullptr;
+  cudaGraphExec_t& ge = h->graph_exec[kind][par];
+  if (ge && h->graph_max_iters[kind][par] == h->max_iters) return 0;
+  if (ge) cudaGraphExecDestroy(ge);
+  ge = nullptr;
   cudaGraph_t graph = nullptr;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const uint64_t launches = h->launches;
-  int rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
-  if (!rc) rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
-  h->graph_launches[par] = h->launches - launches;
+  int rc = 0;
+  for (uint32_t k = 0; k < clsph_gpu::kGraphLen[kind] && !rc; ++k) rc = enqueue_substep(h, CLSPH_STAGE_ADVECT);
+  h->graph_launches[kind][par] = h->launches - launches;
   h->launches = launches;
   cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
   if (rc) {
@@ -192,13 +194,13 @@ int ensure_graph(clsph_gpu* h) {
     return rc;
   }
   if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&h->graph_exec[par], graph, 0);
+  e = cudaGraphInstantiate(&ge, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
-    h->graph_exec[par] = nullptr;
+    ge = nullptr;
     return fail(CLSPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   }
-  h->graph_max_iters[par] = h->max_iters;
+  h->graph_max_iters[kind][par] = h->max_iters;
   return 0;
 }
 
@@ -547,12 +549,16 @@ int clsph_gpu_step(clsph_gpu* h, uint32_t substeps) {
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step: upload particles first");
   uint32_t done = 0;
   if (h->use_graph && !h->profiling && substeps >= 2) {
-    int rc = ensure_graph(h);
-    if (rc) return rc;
-    for (; done + 2 <= substeps; done += 2) {
-      CUDA_TRY(cudaGraphLaunch(h->graph_exec[h->ids_sel], h->stream));
-      h->launches += h->graph_launches[h->ids_sel];
-      h->substeps += 2;
+    for (int kind = 1; kind >= 0; --kind) {  // the long graph first
+      const uint32_t len = clsph_gpu::kGraphLen[kind];
+      if (substeps - done < len) continue;
+      int rc = ensure_graph(h, kind);
+      if (rc) return rc;
+      for (; done + len <= substeps; done += len) {
+        CUDA_TRY(cudaGraphLaunch(h->graph_exec[kind][h->ids_sel], h->stream));
+        h->launches += h->graph_launches[kind][h->ids_sel];
+        h->substeps += len;
+      }
     }
   }
   for (; done < substeps; ++done) {

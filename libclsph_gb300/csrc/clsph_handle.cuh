@@ -151,11 +151,15 @@ struct clsph_gpu {
   bool have_fields = false;
   uint32_t max_iters = 1024;
 
-  // CUDA graphs of two substeps, one per buffer the particle ids start in
+  // CUDA graphs of a few substeps, one per buffer the particle ids start in
   bool use_graph = false;
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
-  uint32_t graph_max_iters[2] = {0, 0};
-  uint64_t graph_launches[2] = {0, 0};  // kernels in one replay of each graph
+  // [length kind][particle-id buffer]: kind 0 replays 2 substeps, kind 1 16
+  // (long runs of small scenes are otherwise bound by the host's graph
+  // launches)
+  static constexpr uint32_t kGraphLen[2] = {2, 16};
+  cudaGraphExec_t graph_exec[2][2] = {};
+  uint32_t graph_max_iters[2][2] = {};
+  uint64_t graph_launches[2][2] = {};  // kernels in one replay of each graph
 
   // buffers of the learned stepper (clsph_learned.cu), made on first use
   void* learned = nullptr;
@@ -215,10 +219,11 @@ struct clsph_gpu {
   }
 
   void drop_graph() {
-    for (auto& g : graph_exec) {
-      if (g) cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+    for (auto& row : graph_exec)
+      for (auto& g : row) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
   }
 };
 

@@ -67,7 +67,7 @@ def test_batched_scene_matches_oracle(gpu_lib, oracle):
         assert np.array_equal(part["density"], ref["density"])
 
 
-@pytest.mark.parametrize("steps", [2, 7])
+@pytest.mark.parametrize("steps", [2, 7, 35])  # 35: two 16-substep replays, one of 2, one launch
 def test_graph_replay_equals_launches(gpu_lib, steps):
     sc = W.small_block(14, seed=70, velocity_sigma=0.4)
     results = []
@@ -81,6 +81,7 @@ def test_graph_replay_equals_launches(gpu_lib, steps):
     assert np.array_equal(results[0][0].view(np.uint8), results[1][0].view(np.uint8))
     assert np.array_equal(results[0][1], results[1][1])
     assert results[0][2]["substeps"] == results[1][2]["substeps"] == 2 * steps
+    assert results[0][2]["launches"] == results[1][2]["launches"]  # replays count their kernels
 
 
 def test_autotune_keeps_state_and_results(gpu_lib):
