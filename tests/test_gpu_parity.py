@@ -130,3 +130,33 @@ def test_no_mesh(gpu_lib, oracle):
         g.step(1)
         out = g.download()
     assert rel_err(out["position"][:, :3], ref.final["position"][:, :3]) <= RTOL
+
+
+def test_wide_grid_four_radix_passes(gpu_lib, oracle):
+    # two blobs about 260 cells apart along x: Morton keys above 2^24, so the
+    # sort takes all four 8-bit passes; sparse grid, no mesh
+    st = W.water_settings(2 * 216)
+    h = float(st.params["h"])
+    rng = np.random.default_rng(41)
+    a = W.lattice((6, 6, 6), 0.5 * h, (0.0, 0.0, 0.0), 0.01, rng)
+    b = W.lattice((6, 6, 6), 0.5 * h, (260 * 2 * h, 0.0, 0.0), 0.01, rng)
+    vel = rng.normal(0.0, 0.2, (2 * 216, 3)).astype(np.float32)
+    parts = W.particles_from_arrays(np.concatenate([a, b]), vel, vel)
+    scene = W.Scene("wide_432", st.params, st.terms, parts, None, 10, {"h": h})
+    ref = oracle.step(scene.params, scene.terms, scene.particles, None)
+    empty = {"vertices": np.zeros(0, np.float32), "indices": np.zeros(0, np.uint32),
+             "face_normals": np.zeros(0, np.float32)}
+    with GpuSolver(scene.params, scene.terms, scene.n, empty) as g:
+        g.upload(scene.particles)
+        g.step(1)
+        assert g.sync() == 0
+        keys, perm = g.keys()
+        table = g.cell_table()
+        out = g.download()
+    assert int(keys.max()) >= 1 << 24  # the fourth pass ran
+    assert np.array_equal(keys, ref.sorted["grid_index"])
+    assert np.array_equal(perm, ref.perm)
+    assert np.array_equal(table, ref.table)
+    for f in ("position", "velocity", "intermediate_velocity"):
+        assert np.array_equal(out[f][:, :3], ref.final[f][:, :3]), f
+    assert np.array_equal(out["density"], ref.final["density"])
