@@ -76,3 +76,21 @@ def test_collision_cap_is_flagged_and_counted(gpu_lib):
         g.upload(parts)
         g.step(1)
         assert g.sync() & WARN_COLLISION_CAP == 0
+
+
+def test_argument_errors_are_reported(gpu_lib):
+    from libclsph_gb300.gpu import ClsphError
+
+    sc = W.small_block(4, seed=54)
+    with pytest.raises(ClsphError):
+        GpuSolver(sc.params, sc.terms, 0, sc.mesh)  # no particles
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        with pytest.raises(ClsphError):
+            g.set_neighbour_search(99)
+        with pytest.raises(ClsphError):
+            g.step(1)  # nothing uploaded yet
+        with pytest.raises(ValueError):
+            g.upload(sc.particles[:-1])  # wrong count
+        g.upload(sc.particles)
+        g.step(1)
+        assert g.sync() == 0
