@@ -33,7 +33,10 @@ constexpr int kRadixWarpSpan = kRadixTile / kRadixWarps;  // 256 keys per warp
 
 // per-substep counters, zeroed by k_grid_setup
 constexpr int kStepCounters = 8;
-enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntWorkForces = 2, kCntRadixTicket = 3 };
+// [kCntCells] occupied cells listed by k_gather, [kCntWorkDensity] cells
+// taken by the cell-warp density search, [kCntRadixTicket] finished count
+// blocks of a small scene's radix pass
+enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntRadixTicket = 3 };
 
 enum : uint32_t {
   kFlagGridOverflow = 1u,
