@@ -345,8 +345,9 @@ def run_reference(args, world, rank) -> None:
 
 
 def learned_evaluation(scene, solver) -> dict | None:
-    """Plain vs learned 4x-dt over the time of 2000 plain substeps (weights
-    from libclsph_gb300/weights/stepper_4dt.npz; skipped when absent)."""
+    """Plain vs learned 4x-dt over the time of 2000 plain substeps, with the 1 %
+    density check and without it (weights from
+    libclsph_gb300/weights/stepper_4dt.npz; skipped when absent)."""
     from libclsph_gb300 import learned as Lm
     from libclsph_gb300.stepper_eval import evaluate
 
@@ -359,6 +360,8 @@ def learned_evaluation(scene, solver) -> dict | None:
     solver.set_graph(False)
     torch.cuda.synchronize()
     r = evaluate(scene, mlp, plain_substeps=2000, dt_mult=4, checkpoints=10, threshold=0.01)
+    # the same network without the density check: every step learned
+    r_free = evaluate(scene, mlp, plain_substeps=2000, dt_mult=4, checkpoints=10, threshold=1e30)
     mlp.close()
     keep = ("plain_sim_s_per_s", "learned_sim_s_per_s", "speedup", "fallback_fraction", "accepted_steps",
             "rejected_steps", "check_deviation_mean", "check_deviation_max", "density_dev",
@@ -372,6 +375,8 @@ def learned_evaluation(scene, solver) -> dict | None:
     out["curve_pos_rms_chaos_h"] = [c["pos_rms_chaos_h"] for c in r["curve"]]
     out["curve_ke_plain"] = [c["ke_plain"] for c in r["curve"]]
     out["curve_ke_learned"] = [c["ke_learned"] for c in r["curve"]]
+    out["no_check"] = {k: r_free[k] for k in ("learned_sim_s_per_s", "plain_sim_s_per_s", "speedup",
+                                              "density_dev", "density_dev_max", "pos_rms_h_final")}
     return out
 
 
