@@ -160,3 +160,49 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         "curve": curve,
     }
     return out
+
+
+def main(argv=None) -> int:
+    """Command line: `--steps K` runs K learned steps of a workload and prints
+    their statistics (a short run to profile the stepper's kernels);
+    `--evaluate` runs the whole plain-versus-learned comparison instead."""
+    import argparse
+    import json
+
+    from . import workloads as W
+
+    scenes = {"dam_break_1m": W.dam_break_1m, "dam_break_32k": W.dam_break_32k}
+    ap = argparse.ArgumentParser(prog="python -m libclsph_gb300.stepper_eval")
+    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(scenes))
+    ap.add_argument("--steps", type=int, default=8, help="learned steps (without --evaluate)")
+    ap.add_argument("--dt-mult", type=int, default=4)
+    ap.add_argument("--threshold", type=float, default=0.01, help="density check; 1e30 disables it")
+    ap.add_argument("--evaluate", action="store_true", help="plain vs learned over 2000 plain substeps")
+    ap.add_argument("--weights", default=None)
+    a = ap.parse_args(argv)
+
+    scene = scenes[a.workload]()
+    mlp = Lm.Mlp.load(a.weights)
+    try:
+        if a.evaluate:
+            r = evaluate(scene, mlp, plain_substeps=2000, dt_mult=a.dt_mult, checkpoints=10,
+                         threshold=a.threshold)
+            r.pop("curve")
+        else:
+            import torch
+
+            with GpuSolver(scene.params, scene.terms, scene.n, scene.mesh) as s:
+                s.upload(scene.particles)
+                st = Lm.step_learned(s, mlp, a.steps, a.dt_mult, a.threshold)
+                s.sync()
+                torch.cuda.synchronize()
+            r = {"workload": scene.name, "particles": scene.n, "steps": a.steps,
+                 "accepted_steps": st.learned_steps, "rejected": st.rejected}
+    finally:
+        mlp.close()
+    print(json.dumps(r))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
