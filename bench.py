@@ -12,7 +12,9 @@ triangles), synthetic and seeded.
   e2e       the same metric through the public C ABI with HOST buffers: each
             step uploads the 80-byte particle AoS from pinned memory, runs
             the substep and downloads the AoS (the reference's per-substep
-            transfer pattern, sph_simulation.cpp:195-197, 339-341).
+            transfer pattern, sph_simulation.cpp:195-197, 339-341); the
+            engine's unpacking and packing kernels read and write the pinned
+            records in place over the host link.
   roofline  the dominant kernel: algorithmic bytes per launch / its mean
             CUDA-event duration, against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (the restatement of the reference's substep,

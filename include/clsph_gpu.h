@@ -128,13 +128,17 @@ int clsph_gpu_set_graph(clsph_gpu* h, int enabled);
 
 /* Replaces the enqueueWriteBuffer of sph_simulation.cpp:195-197: host AoS ->
  * device. `particles` points to n clsph_particle (only position, velocity and
- * intermediate_velocity are read, as in the reference). */
+ * intermediate_velocity are read, as in the reference). Pageable memory is
+ * copied before the call returns; pinned (page-locked, 16-byte aligned)
+ * memory is read by a kernel on the handle's stream, so it must stay
+ * unchanged until the stream gets there, as with any asynchronous copy. */
 int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles);
 
 /* Replaces the enqueueReadBuffer of sph_simulation.cpp:339-341: device -> host
  * AoS in the current (sorted) order, with density, pressure and grid_index of
  * the last substep and acceleration = 0, as the reference leaves them.
- * Synchronises the stream. */
+ * Pinned destinations are written by the packing kernel in place, pageable
+ * ones through a staging copy. Synchronises the stream. */
 int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles);
 
 /* `substeps` calls of simulate_single_frame (sph_simulation.cpp:173-344) with

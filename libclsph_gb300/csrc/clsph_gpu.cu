@@ -517,15 +517,37 @@ int clsph_gpu_set_mesh(clsph_gpu* h, const float* normals, const float* vertices
   return clsph_gpu_set_scene_mesh(h, 0, normals, vertices, vertex_count, indices, faces);
 }
 
+// Device view of `p` when it is pinned host memory that kernels can read and
+// write in place (16-byte aligned for float4 access), else nullptr.
+static void* mapped_host_records(const void* p) {
+  if (reinterpret_cast<uintptr_t>(p) % 16) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // not a pointer CUDA knows: take the copy path
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+static dim3 aos_grid(const clsph_gpu* h) {
+  return dim3(grid_blocks((uint32_t)std::min<size_t>((size_t)h->n * 5, 0xFFFFFFFFu), h->sm_count * 8));
+}
+
+// Pageable records are copied into the staging buffer and unpacked there;
+// pinned records are read by the unpack kernel directly (the host link is
+// the bound either way, and this saves the staging pass).
 int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles) {
   if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "upload: bad argument");
-  CUDA_TRY(cudaMemcpyAsync(h->aos_stage, particles, sizeof(clsph_particle) * h->n,
-                           cudaMemcpyHostToDevice, h->stream));
+  const float4* src = static_cast<const float4*>(mapped_host_records(particles));
+  if (!src) {
+    CUDA_TRY(cudaMemcpyAsync(h->aos_stage, particles, sizeof(clsph_particle) * h->n,
+                             cudaMemcpyHostToDevice, h->stream));
+    src = h->aos_stage;
+  }
   h->launch(K_MISC, k_bbox_reset, dim3(grid_blocks(6 * h->nscenes, 64)), dim3(kBlock), h->bbox,
             h->nscenes);
-  h->launch(K_UNPACK, k_unpack_aos, dim3(grid_blocks(h->n, h->sm_count * 8)), dim3(kBlock),
-            (const float4*)h->aos_stage, h->n, h->st[0], (const uint16_t*)h->scene_of, h->bbox,
-            h->status);
+  h->launch(K_UNPACK, k_unpack_aos, aos_grid(h), dim3(kBlock), src, h->n, h->st[0],
+            (const uint16_t*)h->scene_of, h->bbox, h->status);
   h->uploaded = true;
   h->partial = false;
   h->have_fields = false;
@@ -535,11 +557,13 @@ int clsph_gpu_upload(clsph_gpu* h, const clsph_particle* particles) {
 int clsph_gpu_download(clsph_gpu* h, clsph_particle* particles) {
   if (!h || !particles) return fail(CLSPH_ERR_ARGUMENT, "download: bad argument");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "download: no complete state");
-  h->launch(K_PACK, k_pack_aos, dim3(grid_blocks(h->n, h->sm_count * 8)), dim3(kBlock),
-            h->aos_stage, h->n, h->st[0], (const float4*)h->aux, (const uint32_t*)h->keys,
-            (const uint32_t*)h->ctl, h->have_fields ? 1 : 0);
-  CUDA_TRY(cudaMemcpyAsync(particles, h->aos_stage, sizeof(clsph_particle) * h->n,
-                           cudaMemcpyDeviceToHost, h->stream));
+  float4* dst = static_cast<float4*>(mapped_host_records(particles));
+  h->launch(K_PACK, k_pack_aos, aos_grid(h), dim3(kBlock), dst ? dst : h->aos_stage, h->n, h->st[0],
+            (const float4*)h->aux, (const uint32_t*)h->keys, (const uint32_t*)h->ctl,
+            h->have_fields ? 1 : 0);
+  if (!dst)
+    CUDA_TRY(cudaMemcpyAsync(particles, h->aos_stage, sizeof(clsph_particle) * h->n,
+                             cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   return check_launch(h);
 }

@@ -305,54 +305,68 @@ __device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene,
   }
 }
 
-// Host AoS (80-byte particle) -> SoA state, with bounding box.
+// Host AoS (80-byte particle records, 5 float4 each) -> SoA state, with
+// bounding box. One thread per float4 of the record array, so a warp reads
+// 512 contiguous bytes: `aos` is the device staging copy or, for pinned host
+// memory, the caller's records themselves, read over the host link.
 static __global__ void k_unpack_aos(const float4* __restrict__ aos, uint32_t n, State st,
                              const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ bbox,
                              uint32_t* __restrict__ status) {
   const float qnan = __int_as_float(0x7FC00000);
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const uint32_t i = base + threadIdx.x;
+  const size_t words = (size_t)n * 5;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < words; base += stride) {
+    const size_t q = base + threadIdx.x;
     float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
     int scene = -1;
-    if (i < n) {
-    const float4* p = aos + (size_t)i * 5;
-      float4 pos = p[0], vel = p[1], ivel = p[2];
-    pos.w = 0.f;
-    vel.w = 0.f;
-    ivel.w = 0.f;
-    st.pos[i] = pos;
-    st.vel[i] = vel;
-    st.ivel[i] = ivel;
-    lo = make_float3(pos.x, pos.y, pos.z);
-    hi = lo;
-    scene = scene_of[i];
-    if (!(isfinite(pos.x) && isfinite(pos.y) && isfinite(pos.z))) atomicOr(status, kFlagNonFinite);
+    if (q < words) {
+      const uint32_t i = (uint32_t)(q / 5), f = (uint32_t)(q - (size_t)i * 5);
+      if (f < 3) {  // position, velocity, intermediate velocity; the rest is output only
+        float4 v = aos[q];
+        v.w = 0.f;
+        if (f == 0) {
+          st.pos[i] = v;
+          lo = make_float3(v.x, v.y, v.z);
+          hi = lo;
+          scene = scene_of[i];
+          if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) atomicOr(status, kFlagNonFinite);
+        } else if (f == 1) {
+          st.vel[i] = v;
+        } else {
+          st.ivel[i] = v;
+        }
+      }
     }
     bbox_accumulate(lo, hi, scene, bbox);
   }
 }
 
 // SoA -> host AoS: acceleration is 0 after the advection loop (sph.cl:97-99).
+// One thread per float4 of the record array (contiguous stores), into the
+// staging copy or straight into pinned host memory.
 static __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st,
                            const float4* __restrict__ aux, const uint32_t* __restrict__ keys_base,
                            const uint32_t* __restrict__ ctl, int have_fields) {
   const KeySplit split{ctl[kCtlShift]};
   const uint32_t sel = have_fields ? sorted_sel(ctl[kCtlMaxKey]) : 0u;
   const uint32_t* keys = keys_base + (size_t)sel * n;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4* p = aos + (size_t)i * 5;
-    p[0] = st.pos[i];
-    p[1] = st.vel[i];
-    p[2] = st.ivel[i];
-    p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 tail;
-    const float4 a = have_fields ? aux[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    tail.x = a.x;
-    tail.y = a.y;
-    tail.z = __uint_as_float(have_fields ? split.morton(keys[i]) : 0u);
-    tail.w = 0.f;
-    p[4] = tail;
+  const size_t words = (size_t)n * 5;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < words; q += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(q / 5), f = (uint32_t)(q - (size_t)i * 5);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (f == 0) {
+      v = st.pos[i];
+    } else if (f == 1) {
+      v = st.vel[i];
+    } else if (f == 2) {
+      v = st.ivel[i];
+    } else if (f == 4 && have_fields) {  // density, pressure, grid cell code, 0
+      const float4 a = aux[i];
+      v.x = a.x;
+      v.y = a.y;
+      v.z = __uint_as_float(split.morton(keys[i]));
+    }
+    aos[q] = v;
   }
 }
 
