@@ -158,7 +158,7 @@ int clsph_host::enqueue_advect(clsph_gpu* h) {
             dim3(kBlock), n, h->st[1],
             (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes, (const Consts*)h->consts,
             (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status, h->capped,
-            (const float4*)nullptr, 1.f, 1.f);
+            (const float4*)nullptr, 1.f, 1.f, (const float4*)nullptr, (const float*)nullptr);
   return 0;
 }
 

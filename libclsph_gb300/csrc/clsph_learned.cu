@@ -6,9 +6,10 @@
 //   k_forces<.., FeatureHook>  the plain forces kernel that also gathers 32
 //                   neighbour features per particle (sorted slot order),
 //                   standardised to BF16 rows
-//   k_mlp_infer     fused BF16 tensor-core MLP -> acceleration correction and
-//                   predicted density
-//   k_advect<true>  one leapfrog + collision pass over dt_mult time steps
+//   k_mlp_tc        fused BF16 MLP on the tcgen05 tensor cores -> the
+//                   network's de-standardised outputs
+//   k_advect<true>  outputs -> acceleration correction and predicted density,
+//                   then one leapfrog + collision pass over dt_mult time steps
 // and, at the next step, k_gate compares the density reached with the
 // prediction to accept the step or roll it back.
 
@@ -231,29 +232,10 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
-// MLP outputs -> physical acceleration correction and predicted density.
-// Each output is first clamped to its training mean +- kOutputClamp standard
-// deviations, which bounds the correction a single step can apply.
-constexpr float kOutputClamp = 4.f;
-struct StoreCorr {
-  float4* corr;
-  const float4* aux;
-  const Consts* consts;
-  const uint16_t* scene_of;
-  const float* y_mu;     // [4]
-  const float* y_sigma;  // [4]
-  __device__ float clamp_out(float v, int k) const {
-    const float lo = y_mu[k] - kOutputClamp * y_sigma[k], hi = y_mu[k] + kOutputClamp * y_sigma[k];
-    return fminf(fmaxf(v, lo), hi);
-  }
-  __device__ void operator()(uint32_t row, float4 y) const {
-    const Consts& c = consts[scene_of[row]];
-    const float dt = c.time_delta * c.scale;
-    const float s = c.h / (dt * dt);
-    corr[row] = make_float4(clamp_out(y.x, 0) * s, clamp_out(y.y, 1) * s, clamp_out(y.z, 2) * s,
-                            aux[row].x * (1.f + clamp_out(y.w, 3)));
-  }
-};
+// The learned step's MLP stores its de-standardised outputs as they are
+// (clsph_nn::StoreRaw); k_advect<true> turns them into the acceleration
+// correction and the predicted density (learned_correction), where the loads
+// it needs for that are hidden by many resident warps.
 
 template <class Store>
 int launch_infer(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows,
@@ -659,15 +641,14 @@ int enqueue_learned_tail(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t d
   fh.xstd = L->x;
   int rc = launch_forces_hooked(h, fh);
   if (rc) return rc;
-  rc = launch_tc(h->stream, h->sm_count, L->x, n, tc_weights(m),
-                     StoreCorr{L->corr, h->aux, h->consts, h->scene_of, m->blob + clsph_nn::kOffYMu,
-                               m->blob + clsph_nn::kOffYSigma},
-                     reinterpret_cast<uint32_t*>(L->dev_sum + 1), h, K_MLP);
+  rc = launch_tc(h->stream, h->sm_count, L->x, n, tc_weights(m), clsph_nn::StoreRaw{L->corr},
+                 reinterpret_cast<uint32_t*>(L->dev_sum + 1), h, K_MLP);
   if (rc) return rc;
   h->launch(K_LEARNED_ADVECT, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
             dim3(kBlock), n, h->st[1], (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes,
             (const Consts*)h->consts, (const uint16_t*)h->scene_of, h->max_iters, h->bbox, h->status,
-            h->capped, (const float4*)L->corr, (float)dt_mult, position_weight(dt_mult));
+            h->capped, (const float4*)L->corr, (float)dt_mult, position_weight(dt_mult),
+            (const float4*)h->aux, (const float*)(m->blob + clsph_nn::kOffYMu));
   return 0;
 }
 
@@ -1017,7 +998,8 @@ int collect_level(clsph_collector* c, float* level) {
   h->launch(K_MISC, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)), dim3(kBlock),
             n, h->st[1], (const float4*)h->acc, c->scratch, (const DevMesh*)h->meshes, (const Consts*)h->consts,
             (const uint16_t*)h->scene_of, h->max_iters, c->sbbox, c->sstatus, c->scapped,
-            (const float4*)c->zero, (float)c->dt_mult, position_weight(c->dt_mult));
+            (const float4*)c->zero, (float)c->dt_mult, position_weight(c->dt_mult), (const float4*)nullptr,
+            (const float*)nullptr);
   h->launch(K_MISC, k_ring_naive, dim3(grid_blocks(n)), dim3(kBlock), n, (const uint32_t*)h->ids[h->ids_sel],
             c->stride, c->m, (const float4*)c->scratch.ivel, (const Consts*)h->consts,
             (const uint16_t*)h->scene_of, level);

@@ -148,6 +148,33 @@ struct GeluConsts {
   __device__ uint32_t operator()(float a, float b) const { return gelu2_bf16(a, b, k0, k01, hf); }
 };
 
+// Twice gelu2_bf16, exactly: x (1 + tanh u) = fma(x, t, x) is the same
+// rounding of twice 0.5 x (1 + tanh u) (a power-of-two factor commutes with
+// rounding), one multiplication fewer. The tcgen05 kernel uses it with the
+// next layer's BF16 weights halved (Bf16Weights::w2t, w3t), so every product
+// of the layer is unchanged.
+__device__ __forceinline__ uint32_t gelu2x2_bf16(float2 v, uint32_t k0, uint32_t k01) {
+  const uint32_t x = pack_bf16(v.x, v.y);
+  uint32_t x2, c, u, t, r;
+  asm("mul.rn.bf16x2 %0, %1, %1;\n" : "=r"(x2) : "r"(x));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;\n" : "=r"(c) : "r"(x2), "r"(k01), "r"(k0));
+  asm("mul.rn.bf16x2 %0, %1, %2;\n" : "=r"(u) : "r"(x), "r"(c));
+  asm("tanh.approx.bf16x2 %0, %1;\n" : "=r"(t) : "r"(u));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;\n" : "=r"(r) : "r"(x), "r"(t));
+  return r;
+}
+
+struct GeluTwiceConsts {
+  uint32_t k0, k01;
+  __device__ GeluTwiceConsts()
+      : k0(pack_bf16(0.7978845608028654f, 0.7978845608028654f)),
+        k01(pack_bf16(0.7978845608028654f * 0.044715f, 0.7978845608028654f * 0.044715f)) {}
+  // two accumulator values + their biases (one packed FP32 addition)
+  __device__ uint32_t operator()(float2 acc, float2 bias) const {
+    return gelu2x2_bf16(__fadd2_rn(acc, bias), k0, k01);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Fused inference on the warp-level mma.sync path (cross-check of the
 // tcgen05 kernel in clsph_mlp_tc.cuh)
@@ -577,6 +604,9 @@ __global__ void k_reduce_splits(const float* __restrict__ ws, int splits, size_t
 // BF16 copies of the weights used by the kernels: W1, W2 as stored
 // ([in][out], training GEMMs and the mma.sync path), W1t, W2t transposed
 // ([out][in], tcgen05 operands), W3 padded to 8 columns.
+// BF16 copies of the weights: w1..w3 for the mma.sync kernels and training,
+// w1t..w3t transposed for the tcgen05 kernel, whose w2t and w3t hold half the
+// weights (its activations are twice GELU, gelu2x2_bf16).
 struct Bf16Weights {
   bf16* w1;
   bf16* w2;
@@ -586,17 +616,18 @@ struct Bf16Weights {
   bf16* w3t;  // [16][256], rows 4..15 zero
   __device__ void put(int i, float v) const {
     const bf16 b = __float2bfloat16_rn(v);
+    const bf16 half = __float2bfloat16_rn(0.5f * v);  // = b / 2 exactly for |v| >= 2^-125
     if (i < kOffB1) {
       w1[i] = b;
       w1t[(i % kHid) * kIn + i / kHid] = b;
     } else if (i >= kOffW2 && i < kOffB2) {
       const int j = i - kOffW2;
       w2[j] = b;
-      w2t[(j % kHid) * kHid + j / kHid] = b;
+      w2t[(j % kHid) * kHid + j / kHid] = half;
     } else if (i >= kOffW3 && i < kOffB3) {
       const int j = i - kOffW3;
       w3[(j / kOut) * kOutPad + j % kOut] = b;
-      w3t[(j % kOut) * kHid + j / kOut] = b;
+      w3t[(j % kOut) * kHid + j / kOut] = half;
     }
   }
 };

@@ -3,19 +3,26 @@
 // One persistent CTA of 16 warps per SM, 128-row tiles. All three weight
 // matrices live in shared memory for the whole launch (W2 128 KB, W1 16 KB,
 // W3 padded to 16 outputs 8 KB; canonical no-swizzle K-major core-matrix
-// layout); accumulators live in tensor memory (layer 1 and layer 3 in
-// columns 0..255, layer 2 in columns 256..511 of a 512-column allocation).
-// Per tile:
-//   all threads   X rows (loaded into registers during the previous tile's
-//                 layer-2 MMAs) -> shared memory, the A operand of layer 1
-//   thread 0      2 x tcgen05.mma M128 N256 K16 -> TMEM, tcgen05.commit -> mbarrier
-//   16 warps      tcgen05.ld, + b1, GELU, BF16 -> shared memory (A of layer 2)
-//   thread 0      16 x tcgen05.mma M128 N256 K16, commit
-//   16 warps      tcgen05.ld, + b2, GELU, BF16 -> shared memory (A of layer 3)
-//   thread 0      16 x tcgen05.mma M128 N16 K16, commit
-//   4 warps       tcgen05.ld of the 4 outputs, + b3, de-standardised, Store hook.
-// Every mbarrier wait is bounded; a wait that runs out sets *err, the CTA
-// leaves its tile loop, waits (bounded) for its own MMAs and frees TMEM.
+// layout). A tile needs one 256-column region of tensor memory for its whole
+// life: the layer-1 accumulator, then the layer-2 accumulator over it, then
+// the layer-2 activations packed as BF16 over that (the A operand of layer 3,
+// read by the MMA straight from tensor memory) and the layer-3 accumulator in
+// columns the packing leaves free. Two regions (512 columns) hold two tiles,
+// so the CTA runs a two-tile pipeline; per step u (tile c = u-th tile of the
+// CTA, region u % 2):
+//   16 warps   wait L3(u-2); outputs of tile u-2 (+ b3, de-standardised,
+//              Store hook; 4 warps); X rows of c -> shared memory
+//   thread 0   L1(c): 2 x tcgen05.mma M128 N256 K16 -> region, commit -> bar_l1
+//   16 warps   wait L2(u-1) (frees the shared activation tile); wait L1(c);
+//              tcgen05.ld, + b1, GELU, BF16 -> shared memory (A of layer 2)
+//   thread 0   L2(c): 16 x M128 N256 K16 -> region, commit -> bar_l2
+//   16 warps   tile u-1: tcgen05.ld, + b2, GELU, BF16, tcgen05.st in place
+//              (while L2(c) runs on the tensor pipe)
+//   thread 0   L3(u-1): 16 x M128 N16 K16, A from tensor memory, commit -> bar_l3
+// so layer 2 of one tile runs under the epilogue of the other. Each mbarrier
+// gets one commit and one wait per tile, so a wait never meets a phase that
+// completed twice. Every wait is bounded; a wait that runs out sets *err, the
+// CTA leaves its tile loop, waits (bounded) for its own MMAs and frees TMEM.
 //
 // Encodings (PTX ISA, tcgen05): shared-memory descriptor = start address >> 4
 // in bits 0-13, leading-dimension byte offset >> 4 in 16-29 (distance between
@@ -23,7 +30,9 @@
 // 32-45 (distance between 8-row groups), descriptor version 1 in 46-47,
 // layout type 0 (no swizzle) in 61-63. Instruction descriptor for kind::f16:
 // D format F32 (bits 4-5 = 1), A and B BF16 (7-9 = 1, 10-12 = 1), both
-// K-major (15, 16 = 0), N >> 3 in 17-22, M >> 4 in 24-28.
+// K-major (15, 16 = 0), N >> 3 in 17-22, M >> 4 in 24-28. An A operand in
+// tensor memory holds row r in lane r and two BF16 of consecutive K per
+// 32-bit column (a K = 16 slice is 8 columns).
 #pragma once
 
 #include "clsph_mlp.cuh"
@@ -43,8 +52,8 @@ constexpr uint32_t kTcW3 = kTcX + kTcRows * kIn * 2;     // 16 x 256 bf16, SBO 4
 constexpr uint32_t kTcB1 = kTcW3 + kOut3 * kHid * 2;     // fp32 [256]
 constexpr uint32_t kTcB2 = kTcB1 + kHid * 4;             // fp32 [256]
 constexpr uint32_t kTcMisc = kTcB2 + kHid * 4;           // b3, y_mu, y_sigma [4 each]
-constexpr uint32_t kTcBar = kTcMisc + 48;                // mbarrier (8 B)
-constexpr uint32_t kTcSlot = kTcBar + 8;                 // TMEM base address (4 B)
+constexpr uint32_t kTcBar = kTcMisc + 48;                // mbarriers bar_l1, bar_l2, bar_l3 (8 B each)
+constexpr uint32_t kTcSlot = kTcBar + 24;                // TMEM base address (4 B)
 constexpr uint32_t kTcSmem = kTcSlot + 8;
 static_assert(kTcSmem <= 232448, "shared memory of the tcgen05 MLP");
 
@@ -53,6 +62,9 @@ constexpr uint32_t tc_idesc(int m, int n) {
 }
 constexpr uint32_t kTcIdesc = tc_idesc(kTcRows, kHid);
 constexpr uint32_t kTcIdesc3 = tc_idesc(kTcRows, kOut3);
+// tensor-memory columns within a tile's 256-column region
+constexpr uint32_t kTcRegion = 256;
+constexpr uint32_t kTcAcc3 = 32;  // layer-3 accumulator: columns the packing leaves free
 constexpr uint32_t kTcWaitLimit = 1u << 24;
 
 struct TcWeights {
@@ -77,6 +89,15 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// the same with the A operand in tensor memory at column address tmem_a
+__device__ __forceinline__ void tc_mma_tmem_a(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
@@ -126,6 +147,21 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 64 consecutive 32-bit TMEM columns of this thread's lane: one load and one
+// wait in a single asm statement, so no use of the values can move above the
+// wait and the load latency is paid once per 64 columns
+__device__ __forceinline__ void tc_ld64(uint32_t taddr, float (&v)[64]) {
+  uint32_t r[64];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 64; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 // 4 consecutive 32-bit TMEM columns of this thread's lane
 __device__ __forceinline__ void tc_ld4(uint32_t taddr, float (&v)[4]) {
   uint32_t r[4];
@@ -137,6 +173,17 @@ __device__ __forceinline__ void tc_ld4(uint32_t taddr, float (&v)[4]) {
   for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 16 consecutive 32-bit TMEM columns of this thread's lane <- v
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+      "%13, %14, %15, %16};\n" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+      "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
                "r"(v.w)
@@ -146,24 +193,43 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
 // TMEM columns [col0, col0 + 64) of this thread's row -> + bias, GELU, BF16
 // -> the row's K slice of the canonical A-operand tile at `tile` (K = 256)
 __device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, int col0, const float* bias, uint32_t tile,
-                                                   int r, const GeluConsts& gelu) {
-#pragma unroll 1
-  for (int c = 0; c < 2; ++c) {
-    const int cb = col0 + c * 32;
-    float v[32];
-    tc_ld32(taddr + cb, v);
+                                                   int r, const GeluTwiceConsts& gelu) {
+  const float2* bias2 = reinterpret_cast<const float2*>(bias);
+  float v[64];
+  tc_ld64(taddr + col0, v);
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      uint32_t p[4];
+  for (int e = 0; e < 8; ++e) {
+    uint32_t p[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int k = e * 8 + 2 * q;
-        p[q] = gelu(v[k] + bias[cb + k], v[k + 1] + bias[cb + k + 1]);
-      }
-      st_shared_v4(tile + (r >> 3) * 4096 + ((cb + e * 8) >> 3) * 128 + (r & 7) * 16,
-                   make_uint4(p[0], p[1], p[2], p[3]));
+    for (int q = 0; q < 4; ++q) {
+      const int k = e * 8 + 2 * q;
+      p[q] = gelu(make_float2(v[k], v[k + 1]), bias2[(col0 + k) >> 1]);
     }
+    st_shared_v4(tile + (r >> 3) * 4096 + ((col0 + e * 8) >> 3) * 128 + (r & 7) * 16,
+                 make_uint4(p[0], p[1], p[2], p[3]));
   }
+}
+
+// TMEM columns [taddr, taddr + 64) of this thread's row -> + bias, GELU, BF16
+// pairs -> back into columns [taddr, taddr + 32) once all 64 are read, which
+// makes the activations of these 64 K an A operand in tensor memory
+__device__ __forceinline__ void tc_hidden_in_place(uint32_t taddr, const float* bias,
+                                                   const GeluTwiceConsts& gelu) {
+  const float2* bias2 = reinterpret_cast<const float2*>(bias);
+  float v[64];
+  tc_ld64(taddr, v);
+  uint32_t p[32];
+#pragma unroll
+  for (int q = 0; q < 32; ++q) p[q] = gelu(make_float2(v[2 * q], v[2 * q + 1]), bias2[q]);
+  tc_st16(taddr, reinterpret_cast<const uint32_t(&)[16]>(p[0]));
+  tc_st16(taddr + 16u, reinterpret_cast<const uint32_t(&)[16]>(p[16]));
+}
+
+// column of the K = 16 slice `ks` of the packed layer-2 activations within a
+// region: the 64-column chunk of warp column quarter ks / 4, whose first 32
+// columns hold its 64 values
+__device__ __forceinline__ uint32_t tc_h2_col(int ks) {
+  return 64u * (uint32_t)(ks >> 2) + 8u * (uint32_t)(ks & 3);
 }
 
 template <class Store>
@@ -175,7 +241,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   float* s_b1 = reinterpret_cast<float*>(smem + kTcB1);
   float* s_b2 = reinterpret_cast<float*>(smem + kTcB2);
   float* s_misc = reinterpret_cast<float*>(smem + kTcMisc);
-  const uint32_t bar = sb + kTcBar;
+  const uint32_t bar_l1 = sb + kTcBar, bar_l2 = bar_l1 + 8, bar_l3 = bar_l1 + 16;
 
   // weights -> canonical K-major core-matrix layout: element (row, k) at
   // (row / 8) * SBO + (k / 8) * 128 + (row % 8) * 16 + (k % 8) * 2
@@ -207,7 +273,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    for (uint32_t b = bar_l1; b <= bar_l3; b += 8)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   fence_async_smem();
@@ -219,87 +286,108 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int lg = warp & 3, cq = warp >> 2;                      // lane quarter, column quarter
   const int r = lg * 32 + lane;                                  // tile row = TMEM lane
   const uint32_t t_row = tmem + ((uint32_t)(lg * 32) << 16);
-  const GeluConsts gelu;
-  uint32_t phase = 0;
+  const GeluTwiceConsts gelu;  // twice GELU: W2 and W3 are stored halved
+  // one phase bit and one count of unwaited commits (thread 0) per barrier
+  uint32_t ph1 = 0, ph2 = 0, ph3 = 0, n1 = 0, n2 = 0, n3 = 0;
   bool ok = true;
-  uint32_t issued = 0;  // commits made by thread 0 and not yet waited for
   const uint32_t tiles = (rows + kTcRows - 1) / kTcRows;
+  const uint32_t mine = blockIdx.x < tiles ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;  // tiles of this CTA
+  auto tile_of = [&](uint32_t u) { return blockIdx.x + u * gridDim.x; };
+  auto region = [&](uint32_t u) { return (u & 1u) * kTcRegion; };
   // this thread's 16-byte chunk of a tile's X rows: row tid / 4, chunk tid % 4
   const int xr = tid >> 2, xc = tid & 3;
   const uint32_t x_dst = sb + kTcX + (xr >> 3) * 512 + xc * 128 + (xr & 7) * 16;
-  auto load_x = [&](uint32_t tile) {
-    const uint32_t row = tile * kTcRows + xr;
-    return (tile < tiles && row < rows) ? reinterpret_cast<const uint4*>(x)[(size_t)row * (kIn / 8) + xc]
-                                        : make_uint4(0u, 0u, 0u, 0u);
+  auto load_x = [&](uint32_t u) {
+    const uint32_t row = tile_of(u) * kTcRows + xr;
+    return (u < mine && row < rows) ? reinterpret_cast<const uint4*>(x)[(size_t)row * (kIn / 8) + xc]
+                                    : make_uint4(0u, 0u, 0u, 0u);
   };
-  auto wait_all = [&]() {
-    const bool got = tc_wait(bar, phase);
-    phase ^= 1;
-    if (tid == 0 && got) --issued;
+  // a wait that runs out keeps its phase, so the teardown waits for the same one
+  auto wait_on = [&](uint32_t b, uint32_t& ph, uint32_t& pending) {
+    const bool got = tc_wait(b, ph);
+    if (got) {
+      ph ^= 1;
+      if (tid == 0) --pending;
+    }
     return __syncthreads_and(got);
   };
-  uint4 xv = load_x(blockIdx.x);
-  for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    const uint32_t row0 = tile * kTcRows;
-    st_shared_v4(x_dst, xv);
-    fence_async_smem();
+  uint4 xv = load_x(0);
+  for (uint32_t u = 0; u < mine + 2 && ok; ++u) {
+    const bool cur = u < mine;  // tile u gets layers 1 and 2 in this step
+    if (u >= 2) {               // tile u - 2: outputs
+      if (!(ok = wait_on(bar_l3, ph3, n3))) break;
+      tc_fence_after();
+      if (cq == 0) {
+        float o[4];
+        tc_ld4(t_row + region(u) + kTcAcc3, o);
+        const uint32_t row = tile_of(u - 2) * kTcRows + r;
+        if (row < rows)
+          store(row, make_float4((o[0] + s_misc[0]) * s_misc[8] + s_misc[4],
+                                 (o[1] + s_misc[1]) * s_misc[9] + s_misc[5],
+                                 (o[2] + s_misc[2]) * s_misc[10] + s_misc[6],
+                                 (o[3] + s_misc[3]) * s_misc[11] + s_misc[7]));
+      }
+    }
+    if (cur) {
+      st_shared_v4(x_dst, xv);
+      fence_async_smem();
+    }
     tc_fence_before();
     __syncthreads();
-    if (tid == 0) {
+    if (cur && tid == 0) {  // L1(u) into the region tile u - 2 has just left
       tc_fence_after();
 #pragma unroll
       for (int ks = 0; ks < kIn / 16; ++ks)
-        tc_mma(tmem, tc_desc(sb + kTcX + ks * 256, 128, 512), tc_desc(sb + kTcW1 + ks * 256, 128, 512),
-               kTcIdesc, ks > 0);
-      tc_commit(bar);
-      ++issued;
+        tc_mma(tmem + region(u), tc_desc(sb + kTcX + ks * 256, 128, 512),
+               tc_desc(sb + kTcW1 + ks * 256, 128, 512), kTcIdesc, ks > 0);
+      tc_commit(bar_l1);
+      ++n1;
     }
-    if (!(ok = wait_all())) break;
-    tc_fence_after();
-    tc_hidden_epilogue(t_row, cq * 64, s_b1, sb + kTcH, r, gelu);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+    if (cur) xv = load_x(u + 1);  // next tile's rows, in flight during this step
+    if (u >= 1 && u <= mine) {    // L2(u - 1) done: the shared activation tile is free
+      if (!(ok = wait_on(bar_l2, ph2, n2))) break;
+    }
+    if (cur) {
+      if (!(ok = wait_on(bar_l1, ph1, n1))) break;
       tc_fence_after();
+      tc_hidden_epilogue(t_row + region(u), cq * 64, s_b1, sb + kTcH, r, gelu);
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {  // L2(u) over layer 1's accumulator, which the epilogue has read
+        tc_fence_after();
 #pragma unroll
-      for (int ks = 0; ks < kHid / 16; ++ks)
-        tc_mma(tmem + 256, tc_desc(sb + kTcH + ks * 256, 128, 4096),
-               tc_desc(sb + kTcW2 + ks * 256, 128, 4096), kTcIdesc, ks > 0);
-      tc_commit(bar);
-      ++issued;
+        for (int ks = 0; ks < kHid / 16; ++ks)
+          tc_mma(tmem + region(u), tc_desc(sb + kTcH + ks * 256, 128, 4096),
+                 tc_desc(sb + kTcW2 + ks * 256, 128, 4096), kTcIdesc, ks > 0);
+        tc_commit(bar_l2);
+        ++n2;
+      }
     }
-    xv = load_x(tile + gridDim.x);  // next tile's rows, in flight during the layer-2 MMAs
-    if (!(ok = wait_all())) break;
-    tc_fence_after();
-    tc_hidden_epilogue(t_row + 256, cq * 64, s_b2, sb + kTcH, r, gelu);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+    if (u >= 1 && u <= mine) {  // tile u - 1: layer-2 epilogue under L2(u), then L3(u - 1)
+      const uint32_t reg = region(u - 1);
       tc_fence_after();
+      tc_hidden_in_place(t_row + reg + 64u * cq, s_b2 + 64 * cq, gelu);
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
 #pragma unroll
-      for (int ks = 0; ks < kHid / 16; ++ks)
-        tc_mma(tmem, tc_desc(sb + kTcH + ks * 256, 128, 4096), tc_desc(sb + kTcW3 + ks * 256, 128, 4096),
-               kTcIdesc3, ks > 0);
-      tc_commit(bar);
-      ++issued;
-    }
-    if (!(ok = wait_all())) break;
-    tc_fence_after();
-    if (cq == 0) {
-      float o[4];
-      tc_ld4(t_row, o);
-      if (row0 + r < rows)
-        store(row0 + r, make_float4((o[0] + s_misc[0]) * s_misc[8] + s_misc[4],
-                                    (o[1] + s_misc[1]) * s_misc[9] + s_misc[5],
-                                    (o[2] + s_misc[2]) * s_misc[10] + s_misc[6],
-                                    (o[3] + s_misc[3]) * s_misc[11] + s_misc[7]));
+        for (int ks = 0; ks < kHid / 16; ++ks)
+          tc_mma_tmem_a(tmem + reg + kTcAcc3, tmem + reg + tc_h2_col(ks),
+                        tc_desc(sb + kTcW3 + ks * 256, 128, 4096), kTcIdesc3, ks > 0);
+        tc_commit(bar_l3);
+        ++n3;
+      }
     }
   }
-  // teardown: MMAs of this CTA must be complete before TMEM is freed
-  if (tid == 0 && issued) {
-    if (!tc_wait(bar, phase)) atomicOr(err, 2u);
+  // teardown: MMAs of this CTA must be complete before TMEM is freed (a
+  // commit tracks every MMA issued before it; each barrier's oldest unwaited
+  // commit is the phase to wait for)
+  if (tid == 0) {
+    if (n1 && !tc_wait(bar_l1, ph1)) atomicOr(err, 2u);
+    if (n2 && !tc_wait(bar_l2, ph2)) atomicOr(err, 2u);
+    if (n3 && !tc_wait(bar_l3, ph3)) atomicOr(err, 2u);
   }
   if (!ok && tid == 0) atomicOr(err, 1u);
   tc_fence_before();
