@@ -51,8 +51,8 @@ sys.path.insert(0, str(ROOT))
 # its inputs and outputs, neighbour re-reads excluded)
 ALG_BYTES_PER_PARTICLE = {
     "keys": 16 + 4,                 # read position, write key
-    "radix_scatter": 16,            # read key+slot, write key+slot (per pass)
-    "radix_count": 4,               # read key (per pass)
+    "radix_sweep": 16,              # read key+slot, write key+slot (per pass)
+    "radix_hist": 4,                # read key (once for all passes)
     "gather": 4 + 48 + 48 + 8,      # read slot, read + write state, ids
     "density": 16 + 8,              # read position, write density + pressure
     "forces": 32 + 8 + 16,          # read position, velocity, density, pressure; write acceleration

@@ -35,7 +35,7 @@ int fail(int code, const std::string& msg) {
 }
 
 const char* kKernelNames[K_NUM_CLASSES] = {
-    "grid_setup", "keys",       "radix_count", "radix_scan",     "radix_scatter", "gather",
+    "grid_setup", "keys",       "radix_hist",  "radix_sweep",    "gather",
     "density",    "forces",     "advect",      "unpack_aos",     "pack_aos",      "misc",
     "features",   "mlp",        "learned_advect", "gate"};
 
@@ -86,16 +86,12 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n,
             (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, h->ctl, h->keys);
   if (until <= CLSPH_STAGE_GRID) return 0;
-  for (int pass = 0; pass < 4; ++pass) {
-    h->launch(K_RADIX_COUNT, k_radix_count, dim3(h->ntiles), dim3(kRadixThreads),
-              (const uint32_t*)h->keys, n, pass, cctl, h->tile_hist, h->ntiles, h->digit_total,
-              h->step_counters + kCntRadixTicket);
-    if (h->ntiles > kRadixFuseScanTiles)
-      h->launch(K_RADIX_SCAN, k_radix_scan, dim3(256), dim3(kRadixThreads), h->tile_hist, h->ntiles,
-                pass, cctl, (const uint32_t*)h->digit_total);
-    h->launch(K_RADIX_SCATTER, k_radix_scatter, dim3(h->ntiles), dim3(kRadixThreads), h->keys,
-              h->vals, n, pass, cctl, (const uint32_t*)h->tile_hist, h->ntiles);
-  }
+  h->launch(K_RADIX_HIST, k_radix_hist, dim3(grid_blocks((n + 3) / 4, h->sm_count * 4)), dim3(kRadixThreads),
+            (const uint32_t*)h->keys, n, cctl, h->digit_total, h->lookback, h->ntiles);
+  for (int pass = 0; pass < 4; ++pass)
+    h->launch(K_RADIX_SWEEP, k_radix_onesweep, dim3(h->ntiles), dim3(kRadixThreads), h->keys, h->vals, n,
+              pass, cctl, (const uint32_t*)h->digit_total, h->lookback, h->ntiles,
+              h->step_counters + kCntRadixTile + pass, h->status);
   const int src_ids = h->ids_sel, dst_ids = h->ids_sel ^ 1;
   h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grids,
             (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
@@ -376,7 +372,7 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
       (rc = dev_alloc(&h->nlist, (size_t)h->nlist_cap * n)) || (rc = dev_alloc(&h->ncount, n)) ||
       (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
       (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
-      (rc = dev_alloc(&h->tile_hist, 256 * (size_t)h->ntiles)) ||
+      (rc = dev_alloc(&h->lookback, 4 * 256 * (size_t)h->ntiles)) ||
       (rc = dev_alloc(&h->digit_total, 4 * 256)) || (rc = dev_alloc(&h->ci.keys, slots)) ||
       (rc = dev_alloc(&h->ci.start, slots)) || (rc = dev_alloc(&h->ci.end, slots)) ||
       (rc = dev_alloc(&h->scene_of, n)) || (rc = dev_alloc(&h->grids, nscenes)) ||
@@ -439,7 +435,7 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->ids[s]);
   }
   void* bufs[] = {h->aux,      h->acc,      h->frec,      h->nlist,     h->ncount,      h->cell_list,
-                  h->step_counters, h->keys, h->vals,     h->tile_hist,   h->digit_total,
+                  h->step_counters, h->keys, h->vals,     h->lookback,    h->digit_total,
                   h->ci.keys,  h->ci.start, h->ci.end,    h->scene_of,    h->grids,
                   h->consts,   h->scene_h,  h->meshes,    h->bbox,        h->ctl,
                   h->status,   h->capped,   h->aos_stage};
@@ -612,6 +608,8 @@ int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags) {
   uint32_t f = 0;
   CUDA_TRY(cudaMemcpy(&f, h->status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemset(h->status, 0, sizeof(uint32_t)));
+  if (f & kFlagSortStall)
+    return fail(CLSPH_ERR_CUDA, "sync: a radix sort look-back wait ran out (that substep's order is wrong)");
   if (flags) *flags = f;
   if (h->profiling) h->harvest();
   return CLSPH_OK;

@@ -29,9 +29,8 @@ int fail(int code, const std::string& msg);
 enum KernelClass {
   K_GRID_SETUP,
   K_KEYS,
-  K_RADIX_COUNT,
-  K_RADIX_SCAN,
-  K_RADIX_SCATTER,
+  K_RADIX_HIST,
+  K_RADIX_SWEEP,
   K_GATHER,
   K_DENSITY,
   K_FORCES,
@@ -131,7 +130,7 @@ struct clsph_gpu {
   uint32_t* step_counters = nullptr;  // kStepCounters, zeroed every substep
   uint32_t* keys = nullptr;           // [2n]
   uint32_t* vals = nullptr;           // [2n]
-  uint32_t* tile_hist = nullptr;
+  uint32_t* lookback = nullptr;  // [4 passes][ntiles][256] radix look-back words
   uint32_t ntiles = 0;
   uint32_t* digit_total = nullptr;
   CellIndex ci{};

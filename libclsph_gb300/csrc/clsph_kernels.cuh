@@ -34,14 +34,15 @@ constexpr int kRadixWarpSpan = kRadixTile / kRadixWarps;  // 256 keys per warp
 // per-substep counters, zeroed by k_grid_setup
 constexpr int kStepCounters = 8;
 // [kCntCells] occupied cells listed by k_gather, [kCntWorkDensity] cells
-// taken by the cell-warp density search, [kCntRadixTicket] finished count
-// blocks of a small scene's radix pass
-enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntRadixTicket = 3 };
+// taken by the cell-warp density search, [kCntRadixTile + p] tiles taken by
+// radix pass p
+enum : int { kCntCells = 0, kCntWorkDensity = 1, kCntRadixTile = 4 };
 
 enum : uint32_t {
   kFlagGridOverflow = 1u,
   kFlagCollisionCap = 2u,
   kFlagNonFinite = 4u,
+  kFlagSortStall = 1u << 16,  // internal: a radix look-back wait ran out
 };
 
 struct DevGrid {         // one scene's grid of the current substep
@@ -398,141 +399,91 @@ static __global__ void __launch_bounds__(kBlock)
 }
 
 // ---------------------------------------------------------------- radix sort
-// Stable LSD radix sort of (key, slot) with 8-bit digits: count -> scan ->
-// scatter per pass. Passes beyond DevGrid::passes return at once, so the
-// launch sequence is fixed (graph-capturable) while the work follows the
-// key width. Ping-pong: pass p reads buffer p&1 and writes (p+1)&1.
-// Tiles at or below which the last count block scans the per-tile counts
-// itself (small scenes: the separate scan launch is mostly latency).
-constexpr uint32_t kRadixFuseScanTiles = 64;
+// Stable LSD radix sort of (key, slot) with 8-bit digits in one-sweep form:
+// k_radix_hist reads the keys once and counts the digits of every pass;
+// k_radix_onesweep (one launch per pass) ranks a 2048-key tile in shared
+// memory, publishes the tile's per-digit counts, finds the counts of all
+// earlier tiles by decoupled look-back (each digit's thread walks back over
+// the published words until it meets an inclusive prefix) and scatters.
+// Passes beyond radix_passes return at once, so the launch sequence is fixed
+// (graph-capturable) while the work follows the key width. Ping-pong: pass p
+// reads buffer p&1 and writes (p+1)&1.
+//
+// Look-back words (one per tile and digit, per pass): bits 30-31 the state
+// (0 not yet published, 1 the tile's own count, 2 the inclusive prefix of
+// all tiles up to it), bits 0-29 the value (n < 2^28). Tiles are numbered in
+// the order blocks start (an atomic ticket), so every tile a block waits for
+// belongs to a block that is already running and publishes without waiting
+// itself; the wait is bounded all the same (kRadixLookbackSpins), and a wait
+// that runs out raises kFlagSortStall, which clsph_gpu_sync reports as an
+// error.
+constexpr uint32_t kRadixLookbackSpins = 1u << 20;
+constexpr uint32_t kLbAggregate = 1u << 30, kLbInclusive = 2u << 30, kLbValue = (1u << 30) - 1u;
 
-static __global__ void k_radix_count(const uint32_t* __restrict__ keys_base, uint32_t n, int pass,
-                              const uint32_t* __restrict__ ctl, uint32_t* __restrict__ tile_hist,
-                              uint32_t ntiles, uint32_t* __restrict__ digit_total,
-                              uint32_t* __restrict__ ticket) {
-  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t warp_sums[256 / 32];
-  __shared__ bool last;
-  hist[threadIdx.x] = 0u;
-  __syncthreads();
-  const uint32_t* keys = keys_base + (size_t)(pass & 1) * n;
-  const uint32_t base = blockIdx.x * kRadixTile;
-  const int shift = 8 * pass;
-  // the order of counting does not matter: 16-byte loads, 4 keys each
-  // (scalar loads at the end of the keys and where the second ping-pong
-  // buffer, n keys in, is not 16-byte aligned)
-  static_assert(kRadixItems % 4 == 0, "vector loads of the count kernel");
-#pragma unroll
-  for (int k = 0; k < kRadixItems / 4; ++k) {
-    const uint32_t idx = base + (k * kRadixThreads + threadIdx.x) * 4u;
-    if (idx + 3u < n && (reinterpret_cast<uintptr_t>(keys + idx) & 15u) == 0u) {
-      const uint4 q = __ldg(reinterpret_cast<const uint4*>(keys + idx));
-      atomicAdd(&hist[(q.x >> shift) & 0xFFu], 1u);
-      atomicAdd(&hist[(q.y >> shift) & 0xFFu], 1u);
-      atomicAdd(&hist[(q.z >> shift) & 0xFFu], 1u);
-      atomicAdd(&hist[(q.w >> shift) & 0xFFu], 1u);
-    } else {
-      for (uint32_t e = idx; e < idx + 4u && e < n; ++e) atomicAdd(&hist[(__ldg(&keys[e]) >> shift) & 0xFFu], 1u);
-    }
-  }
-  __syncthreads();
-  uint32_t c = hist[threadIdx.x];
-  tile_hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
-  if (c) atomicAdd(&digit_total[pass * 256 + threadIdx.x], c);
-  if (ntiles > kRadixFuseScanTiles) return;
-  // small scenes: the last block to finish turns the counts into offsets
-  // (what k_radix_scan does), so the scan needs no launch of its own
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1u;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const uint32_t d = threadIdx.x;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t tot = __ldcg(&digit_total[pass * 256 + d]);
-  uint32_t x = tot;  // inclusive scan over the 256 digits
-  for (int off = 1; off < 32; off <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
-    if (lane >= off) x += y;
-  }
-  if (lane == 31) warp_sums[warp] = x;
-  __syncthreads();
-  uint32_t run = x - tot;
-  for (int w = 0; w < warp; ++w) run += warp_sums[w];
-  uint32_t* row = tile_hist + (size_t)d * ntiles;
-  for (uint32_t t = 0; t < ntiles; ++t) {
-    const uint32_t v = __ldcg(&row[t]);
-    row[t] = run;
-    run += v;
-  }
-  if (threadIdx.x == 0) *ticket = 0u;  // for the next pass
+__device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
-// One block per digit: exclusive scan of that digit's per-tile counts plus
-// the number of keys with a smaller digit.
-static __global__ void k_radix_scan(uint32_t* __restrict__ tile_hist, uint32_t ntiles, int pass,
-                             const uint32_t* __restrict__ ctl,
-                             const uint32_t* __restrict__ digit_total) {
-  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
-  __shared__ uint32_t warp_sums[kRadixThreads / 32];
-  __shared__ uint32_t base_s;
-  const uint32_t d = blockIdx.x;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // base = sum of totals of smaller digits
-  uint32_t part = threadIdx.x < d ? digit_total[pass * 256 + threadIdx.x] : 0u;
-  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, off);
-  if (lane == 0) warp_sums[warp] = part;
+// Digit counts of every pass in one read of the keys (16-byte loads), and the
+// look-back words of this substep's passes cleared.
+static __global__ void __launch_bounds__(kRadixThreads)
+    k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ ctl,
+                 uint32_t* __restrict__ digit_total, uint32_t* __restrict__ lookback, uint32_t ntiles) {
+  __shared__ uint32_t hist[4][256];
+  const uint32_t passes = radix_passes(ctl[kCtlMaxKey]);
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) hist[i >> 8][i & 255] = 0u;
+  const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t gstride = (size_t)gridDim.x * blockDim.x;
+  const size_t words = (size_t)passes * ntiles * 256u;
+  for (size_t i = gtid; i < words; i += gstride) lookback[i] = 0u;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t b = 0;
-    for (int w = 0; w < kRadixThreads / 32; ++w) b += warp_sums[w];
-    base_s = b;
+  auto count = [&](uint32_t key) {
+    for (uint32_t p = 0; p < passes; ++p) atomicAdd(&hist[p][(key >> (8 * p)) & 0xFFu], 1u);
+  };
+  const uint32_t n4 = n / 4u;
+  for (size_t q = gtid; q < n4; q += gstride) {
+    const uint4 k = __ldg(reinterpret_cast<const uint4*>(keys) + q);
+    count(k.x);
+    count(k.y);
+    count(k.z);
+    count(k.w);
   }
+  if (gtid < (n & 3u)) count(__ldg(&keys[4u * n4 + gtid]));
   __syncthreads();
-  uint32_t carry = base_s;
-  uint32_t* row = tile_hist + (size_t)d * ntiles;
-  for (uint32_t chunk = 0; chunk < ntiles; chunk += kRadixThreads) {
-    uint32_t idx = chunk + threadIdx.x;
-    uint32_t v = idx < ntiles ? row[idx] : 0u;
-    uint32_t x = v;  // inclusive warp scan
-    for (int off = 1; off < 32; off <<= 1) {
-      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
-      if (lane >= off) x += y;
-    }
-    __syncthreads();
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    uint32_t wbase = 0, total = 0;
-    for (int w = 0; w < kRadixThreads / 32; ++w) {
-      uint32_t s = warp_sums[w];
-      if (w < warp) wbase += s;
-      total += s;
-    }
-    if (idx < ntiles) row[idx] = carry + wbase + x - v;
-    carry += total;
+  for (uint32_t p = 0; p < passes; ++p) {
+    const uint32_t c = hist[p][threadIdx.x];
+    if (c) atomicAdd(&digit_total[p * 256 + threadIdx.x], c);
   }
 }
 
 static __global__ void __launch_bounds__(kRadixThreads)
-    k_radix_scatter(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
-                    int pass, const uint32_t* __restrict__ ctl,
-                    const uint32_t* __restrict__ tile_hist, uint32_t ntiles) {
+    k_radix_onesweep(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
+                     int pass, const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ digit_total,
+                     uint32_t* __restrict__ lookback, uint32_t ntiles, uint32_t* __restrict__ tile_ticket,
+                     uint32_t* __restrict__ status) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t cnt[kRadixWarps][256];
   __shared__ uint32_t tile_off[256];
+  __shared__ uint32_t warp_sums[kRadixWarps];
+  __shared__ uint32_t tile_s;
   const uint32_t* keys_in = keys_base + (size_t)(pass & 1) * n;
   uint32_t* keys_out = keys_base + (size_t)((pass + 1) & 1) * n;
   const uint32_t* vals_in = vals_base + (size_t)(pass & 1) * n;
   uint32_t* vals_out = vals_base + (size_t)((pass + 1) & 1) * n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) tile_s = atomicAdd(tile_ticket, 1u);
   for (int w = 0; w < kRadixWarps; ++w) cnt[w][threadIdx.x] = 0u;
-  tile_off[threadIdx.x] = tile_hist[(size_t)threadIdx.x * ntiles + blockIdx.x];
   __syncthreads();
+  const uint32_t tile = tile_s;
   const int shift = 8 * pass;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t base = blockIdx.x * kRadixTile + warp * kRadixWarpSpan;
+  const uint32_t base = tile * kRadixTile + warp * kRadixWarpSpan;
+  // ranks within the tile: per warp in key order (rows of 32), then warps in order
   uint32_t key[kRadixItems], val[kRadixItems], rank[kRadixItems];
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
@@ -550,20 +501,52 @@ static __global__ void __launch_bounds__(kRadixThreads)
     rank[r] = valid ? ((rk << 8) | d) : 0xFFFFFFFFu;
   }
   __syncthreads();
-  {  // exclusive prefix over warps, per digit
-    uint32_t run = 0;
-    for (int w = 0; w < kRadixWarps; ++w) {
-      uint32_t t = cnt[w][threadIdx.x];
-      cnt[w][threadIdx.x] = run;
-      run += t;
-    }
+  const uint32_t d = threadIdx.x;  // this thread's digit from here on
+  uint32_t local = 0;              // the tile's count of digit d
+  for (int w = 0; w < kRadixWarps; ++w) {
+    const uint32_t t = cnt[w][d];
+    cnt[w][d] = local;
+    local += t;
   }
+  uint32_t* lb = lookback + (size_t)pass * ntiles * 256u;
+  st_relaxed_gpu(&lb[(size_t)tile * 256u + d], (tile == 0 ? kLbInclusive : kLbAggregate) | local);
+  uint32_t excl = 0;  // digit d in all earlier tiles
+  if (tile > 0) {
+    uint32_t t = tile - 1, spins = 0;
+    for (;;) {
+      const uint32_t w = ld_relaxed_gpu(&lb[(size_t)t * 256u + d]);
+      if ((w & ~kLbValue) == 0u) {
+        if (++spins > kRadixLookbackSpins) {
+          atomicOr(status, kFlagSortStall);
+          break;
+        }
+        continue;
+      }
+      excl += w & kLbValue;
+      if ((w & kLbInclusive) || t == 0) break;
+      --t;
+    }
+    st_relaxed_gpu(&lb[(size_t)tile * 256u + d], kLbInclusive | (excl + local));
+  }
+  // keys with a smaller digit: exclusive scan of the pass's digit totals
+  const uint32_t tot = digit_total[pass * 256 + d];
+  uint32_t x = tot;
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  uint32_t below = x - tot;
+  for (int w = 0; w < warp; ++w) below += warp_sums[w];
+  tile_off[d] = below + excl;
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     if (rank[r] == 0xFFFFFFFFu) continue;
-    const uint32_t d = rank[r] & 0xFFu;
-    const uint32_t dst = tile_off[d] + cnt[warp][d] + (rank[r] >> 8);
+    const uint32_t dd = rank[r] & 0xFFu;
+    const uint32_t dst = tile_off[dd] + cnt[warp][dd] + (rank[r] >> 8);
+    if (dst >= n) continue;  // only after a look-back wait ran out (flagged)
     keys_out[dst] = key[r];
     vals_out[dst] = val[r];
   }
