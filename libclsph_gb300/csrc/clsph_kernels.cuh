@@ -468,6 +468,7 @@ static __global__ void __launch_bounds__(kRadixThreads)
                      uint32_t* __restrict__ status) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t cnt[kRadixWarps][256];
+  __shared__ uint32_t hist[256];
   __shared__ uint32_t tile_off[256];
   __shared__ uint32_t warp_sums[kRadixWarps];
   __shared__ uint32_t tile_s;
@@ -478,55 +479,83 @@ static __global__ void __launch_bounds__(kRadixThreads)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) tile_s = atomicAdd(tile_ticket, 1u);
   for (int w = 0; w < kRadixWarps; ++w) cnt[w][threadIdx.x] = 0u;
+  hist[threadIdx.x] = 0u;
   __syncthreads();
   const uint32_t tile = tile_s;
   const int shift = 8 * pass;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t base = tile * kRadixTile + warp * kRadixWarpSpan;
-  // ranks within the tile: per warp in key order (rows of 32), then warps in order
   uint32_t key[kRadixItems], val[kRadixItems], rank[kRadixItems];
+  // the tile's keys and its digit counts, published before the ranking so
+  // that later tiles' look-back finds them as early as possible
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     const uint32_t idx = base + r * 32 + lane;
     const bool valid = idx < n;
     key[r] = valid ? keys_in[idx] : 0u;
     val[r] = valid ? (pass == 0 ? idx : vals_in[idx]) : 0u;
-    const uint32_t d = valid ? ((key[r] >> shift) & 0xFFu) : 256u;
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-    uint32_t rk = 0;
-    if (valid) rk = cnt[warp][d] + __popc(peers & lt_mask);
-    __syncwarp();
-    if (valid && (peers & lt_mask) == 0u) cnt[warp][d] += __popc(peers);
-    __syncwarp();
-    rank[r] = valid ? ((rk << 8) | d) : 0xFFFFFFFFu;
+    if (valid) atomicAdd(&hist[(key[r] >> shift) & 0xFFu], 1u);
   }
   __syncthreads();
-  const uint32_t d = threadIdx.x;  // this thread's digit from here on
-  uint32_t local = 0;              // the tile's count of digit d
-  for (int w = 0; w < kRadixWarps; ++w) {
-    const uint32_t t = cnt[w][d];
-    cnt[w][d] = local;
-    local += t;
-  }
+  const uint32_t d = threadIdx.x;  // this thread's digit in the look-back and the offsets
+  const uint32_t local = hist[d];  // the tile's count of digit d
   uint32_t* lb = lookback + (size_t)pass * ntiles * 256u;
   st_relaxed_gpu(&lb[(size_t)tile * 256u + d], (tile == 0 ? kLbInclusive : kLbAggregate) | local);
+  // ranks within the tile: per warp in key order (rows of 32), then warps in order
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const uint32_t idx = base + r * 32 + lane;
+    const bool valid = idx < n;
+    const uint32_t dr = valid ? ((key[r] >> shift) & 0xFFu) : 256u;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dr);
+    uint32_t rk = 0;
+    if (valid) rk = cnt[warp][dr] + __popc(peers & lt_mask);
+    __syncwarp();
+    if (valid && (peers & lt_mask) == 0u) cnt[warp][dr] += __popc(peers);
+    __syncwarp();
+    rank[r] = valid ? ((rk << 8) | dr) : 0xFFFFFFFFu;
+  }
   uint32_t excl = 0;  // digit d in all earlier tiles
   if (tile > 0) {
-    uint32_t t = tile - 1, spins = 0;
-    for (;;) {
-      const uint32_t w = ld_relaxed_gpu(&lb[(size_t)t * 256u + d]);
-      if ((w & ~kLbValue) == 0u) {
+    // walk back kLookbackWindow tiles per round (independent loads), adding
+    // published counts until an inclusive prefix (tile 0 always has one)
+    constexpr int kLookbackWindow = 4;
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    bool done = false;
+    while (!done) {
+      uint32_t w[kLookbackWindow];
+#pragma unroll
+      for (int k = 0; k < kLookbackWindow; ++k)
+        w[k] = t - k >= 0 ? ld_relaxed_gpu(&lb[(size_t)(t - k) * 256u + d]) : kLbInclusive;
+      int used = 0;
+#pragma unroll
+      for (int k = 0; k < kLookbackWindow; ++k) {
+        if (done || used < k) break;       // stopped at an earlier word of this round
+        if ((w[k] & ~kLbValue) == 0u) break;  // not published yet: load it again
+        excl += w[k] & kLbValue;
+        ++used;
+        if (w[k] & kLbInclusive) done = true;
+      }
+      t -= used;
+      if (!done && used == 0) {
         if (++spins > kRadixLookbackSpins) {
           atomicOr(status, kFlagSortStall);
           break;
         }
-        continue;
+        __nanosleep(32);
       }
-      excl += w & kLbValue;
-      if ((w & kLbInclusive) || t == 0) break;
-      --t;
     }
     st_relaxed_gpu(&lb[(size_t)tile * 256u + d], kLbInclusive | (excl + local));
+  }
+  __syncthreads();
+  {  // per digit: exclusive prefix over warps
+    uint32_t run = 0;
+    for (int w = 0; w < kRadixWarps; ++w) {
+      const uint32_t c = cnt[w][d];
+      cnt[w][d] = run;
+      run += c;
+    }
   }
   // keys with a smaller digit: exclusive scan of the pass's digit totals
   const uint32_t tot = digit_total[pass * 256 + d];
