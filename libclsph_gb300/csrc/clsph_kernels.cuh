@@ -1094,8 +1094,7 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
 struct NoForceHook {
   struct Acc {};
   __device__ __forceinline__ Acc begin(uint32_t) const { return {}; }
-  __device__ __forceinline__ void pair(Acc&, uint32_t, uint32_t, const float4&, const float4&,
-                                       const float4&) const {}
+  __device__ __forceinline__ void pair(Acc&, uint32_t, uint32_t, const V3&, const V3&) const {}
   __device__ __forceinline__ void end(Acc&, uint32_t, const float4&) const {}
 };
 
@@ -1127,7 +1126,10 @@ __global__ void __launch_bounds__(BLOCK)
     const float rr = xnorm(d);
     const float4 vj = make_float4(sj.x, sj.y, sj.z, 0.f);
     force_pair(f, j == i, d, rr, vi, vj, make_float4(0.f, 0.f, pj.w, sj.w), own, hh, lap_b, c);
-    hook.pair(ha, i, j, pi, pj, vj);
+    // the same differences force_pair forms (the compiler shares them); dead
+    // code for the plain substep's empty hook
+    const V3 dv = {XSUB(vj.x, vi.x), XSUB(vj.y, vi.y), XSUB(vj.z, vi.z)};
+    hook.pair(ha, i, j, d, dv);
   };
   auto pair = [&](uint32_t j) { pair_with(j, __ldg(&frec[j]), __ldg(&frec[(size_t)n + j])); };
   const uint32_t cnt = ncount[i];

@@ -61,7 +61,7 @@ struct FeatureHook {
   uint32_t stride, m;
 
   struct Acc {
-    float inv_h, vs, vx, vy, vz;  // vx..vz: the particle's velocity (pair moments)
+    float inv_h, vs;
     float s[22];  // sum w d (3), w d d^T (6), w u (3), w u u^T (6), w d.u, w d x u (3)
     uint32_t cnt;
   };
@@ -71,23 +71,19 @@ struct FeatureHook {
     const Consts& c = consts[scene_of[i]];
     a.inv_h = 1.f / c.h;
     a.vs = c.time_delta * c.scale * a.inv_h;
-    const float4 v = st.vel[i];
-    a.vx = v.x;
-    a.vy = v.y;
-    a.vz = v.z;
 #pragma unroll
     for (int k = 0; k < 22; ++k) a.s[k] = 0.f;
     a.cnt = 0;
     return a;
   }
 
-  // vj: the neighbour's velocity, already loaded by the force evaluation
-  __device__ __forceinline__ void pair(Acc& a, uint32_t i, uint32_t j, const float4& pi, const float4& pj,
-                                       const float4& vj) const {
+  // d = p_i - p_j and dv = v_j - v_i: the force evaluation's own exact
+  // differences (p_j - p_i is exactly -d)
+  __device__ __forceinline__ void pair(Acc& a, uint32_t i, uint32_t j, const V3& d, const V3& dv) const {
     ++a.cnt;
     if (j == i) return;
-    const float dx = (pj.x - pi.x) * a.inv_h, dy = (pj.y - pi.y) * a.inv_h, dz = (pj.z - pi.z) * a.inv_h;
-    const float ux = (vj.x - a.vx) * a.vs, uy = (vj.y - a.vy) * a.vs, uz = (vj.z - a.vz) * a.vs;
+    const float dx = -d.x * a.inv_h, dy = -d.y * a.inv_h, dz = -d.z * a.inv_h;
+    const float ux = dv.x * a.vs, uy = dv.y * a.vs, uz = dv.z * a.vs;
     const float w = fmaxf(0.f, 1.f - (dx * dx + dy * dy + dz * dz));
     a.s[0] += w * dx;
     a.s[1] += w * dy;

@@ -105,6 +105,37 @@ def test_forward_matches_torch(gpu_lib):
     m.close()
 
 
+@pytest.mark.parametrize("tiles_per_cta", [2, 3, 7])
+def test_forward_many_tiles_per_cta(gpu_lib, tiles_per_cta):
+    """Enough rows for several 128-row tiles per persistent CTA, so the
+    tcgen05 kernel's two tensor-memory regions alternate and its two-tile
+    pipeline runs in steady state, with a ragged last tile; it must agree
+    with the mma.sync kernel and with the PyTorch restatement."""
+    blob = random_blob(3 + tiles_per_cta)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rows = sms * 128 * tiles_per_cta - 51
+    g = torch.Generator(device="cuda").manual_seed(tiles_per_cta)
+    x = torch.randn(rows, 32, device="cuda", generator=g).to(torch.bfloat16).contiguous()
+    y = torch.empty(rows, 4, device="cuda", dtype=torch.float32)
+    y_mma = torch.empty_like(y)
+    m = Lm.Mlp(blob=blob)
+    m.forward(x.data_ptr(), rows, y.data_ptr())
+    m.forward_mma_sync(x.data_ptr(), rows, y_mma.data_ptr())
+    torch.cuda.synchronize()
+    assert m.status() == 0
+    with torch.no_grad():
+        fwd, _, t = torch_mlp(blob)
+        ref = fwd(x.float()) * t[Lm.OFF_YSIGMA:] + t[Lm.OFF_YMU:Lm.OFF_YSIGMA]
+    scale = ref.abs().max().item()
+    for got in (y, y_mma):
+        err = (got - ref).abs()
+        assert err.max().item() <= 1e-2 * scale, (err.max().item(), scale)
+        assert err.mean().item() <= 1e-3 * scale, (err.mean().item(), scale)
+    # the two tensor-core paths round the same BF16 products: close to each other
+    assert (y - y_mma).abs().max().item() <= 1e-2 * scale
+    m.close()
+
+
 def test_gradients_match_torch(gpu_lib):
     blob = random_blob(2)
     rows = 4096
