@@ -532,7 +532,7 @@ def main() -> None:
     if not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(scene)
-        except Exception as e:  # the checker failing must not hide the GPU number
+        except Exception as e:  # an oracle failure must not hide the GPU number
             cpu = {"value": None, "unit": "particle-steps/s", "cores": os.cpu_count(),
                    "kind": "port", "sample": f"failed: {e}"}
     line = {

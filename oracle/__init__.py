@@ -1,4 +1,4 @@
-"""ctypes bindings of the CPU checkers — TEST INFRASTRUCTURE.
+"""ctypes bindings of the CPU oracles — TEST INFRASTRUCTURE.
 
 `Oracle` wraps oracle/liboracle.so (the restatement in clsph_oracle.cpp);
 `RefBuild` wraps oracle/_ref/libclsph_ref.so (the reference's own kernel

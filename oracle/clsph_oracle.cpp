@@ -1,7 +1,7 @@
 // CPU oracle for the libclsph per-substep SPH path — TEST INFRASTRUCTURE.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
-// this library, and only as the checker or the timed CPU baseline. The product
+// this library, and only as the oracle or the timed CPU baseline. The product
 // (libclsph_gb300) never links or calls it.
 //
 // It restates, in its own code, what the reference computes for one substep:

@@ -2,7 +2,7 @@
  *
  * A from-scratch restatement (oracle/clsph_oracle.cpp) of the reference's
  * algorithm, used only by tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg as the checker. Nothing in the product links or calls it.
+ * baseline leg as the oracle. Nothing in the product links or calls it.
  *
  * Parity is pinned two ways: (1) against oracle/_ref, the reference's own
  * kernel sources compiled as C++ (bit-exact, development container), and
