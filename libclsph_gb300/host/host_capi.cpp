@@ -84,6 +84,19 @@ int clsph_host_write_houdini(const char* prefix, void* particles, const void* pa
   }
 }
 
+// The same with binary_bgeo set: <prefix>frames/frame0000001.bgeo.
+int clsph_host_write_bgeo(const char* prefix, void* particles, const void* params) {
+  try {
+    houdini_file_saver saver{std::string(prefix)};
+    saver.binary_bgeo = true;
+    simulation_parameters p;
+    std::memcpy(&p, params, sizeof(p));
+    return saver.writeFrameToFile(static_cast<particle*>(particles), p);
+  } catch (const std::exception& e) {
+    return host_fail(e);
+  }
+}
+
 typedef void (*clsph_frame_callback)(void* user, void* particles, const void* params, int full_frame);
 
 // A whole sph_simulation run: load_settings(fluid, params), scene load,

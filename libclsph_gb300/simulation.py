@@ -150,16 +150,74 @@ def density_color(d):
     return f32(r), f32(g), f32(b)
 
 
-class HoudiniFileSaver:
-    """houdini_file_saver (libclsph/file_save_delegates/houdini_file_saver.h:8-20)."""
+def density_colors(d: np.ndarray) -> np.ndarray:
+    """density_color over an array (float32 throughout): (n, 3) RGB."""
+    d = np.asarray(d, dtype=np.float32)
+    one, k500, k1000 = np.float32(1), np.float32(500), np.float32(1000)
+    r = np.where((d > 1000) & (d <= 2000), (d - k1000) / k1000, np.float32(0))
+    g = np.where((d >= 0) & (d < 1000), one - d / k1000, np.float32(0))
+    b = np.where((d >= 500) & (d <= 1000), (d - k500) / k500,
+                 np.where((d >= 1000) & (d <= 1500), one - (d - k1000) / k500, np.float32(0)))
+    return np.stack([r, g, b], axis=1).astype(np.float32)
 
-    def __init__(self, frames_folder_prefix: str):
+
+def bgeo_bytes(particles: np.ndarray, parameters) -> bytes:
+    """One frame as classic binary Houdini geometry (version 5), the file the
+    reference's USE_PARTIO build writes through Partio::write
+    (libclsph/file_save_delegates/houdini_file_saver.cpp:76-88) with the
+    attributes of makeData (util/partio/PartioFunctions.h:5-65): velocity,
+    color (vectors), id (int), mass and pscale (floats) after the position.
+    Big-endian throughout; 16-bit point indices up to 65,535 points, else
+    32-bit. The full velocity is stored (makeData writes only component 0)."""
+    n = int(parameters["particles_count"])
+    be = np.dtype(">i4")
+
+    def name(s: str) -> bytes:
+        return np.array([len(s)], ">u2").tobytes() + s.encode()
+
+    head = b"BgeoV" + np.array([5, n, 1, 0, 0, 5, 0, 1, 0], be).tobytes()
+    for nm, size, typ in (("velocity", 3, 5), ("color", 3, 5), ("id", 1, 1), ("mass", 1, 0),
+                          ("pscale", 1, 0)):
+        head += name(nm) + np.array([size], ">u2").tobytes() + np.array([typ] + [0] * size, be).tobytes()
+    rec = np.dtype([("p", ">f4", 4), ("v", ">f4", 3), ("c", ">f4", 3), ("id", ">i4"), ("m", ">f4"),
+                    ("ps", ">f4")])
+    pts = np.zeros(n, dtype=rec)
+    pts["p"][:, :3] = particles["position"][:n, :3]
+    pts["p"][:, 3] = 1.0
+    pts["v"] = particles["velocity"][:n, :3]
+    pts["c"] = density_colors(particles["density"][:n])
+    pts["id"] = np.arange(n)
+    pts["m"] = np.float32(parameters["particle_mass"])
+    pts["ps"] = np.float32(parameters["h"])
+    prim = (name("generator") + np.array([1], ">u2").tobytes() + np.array([4, 1], be).tobytes() +
+            name("papi") + np.array([0x8000, n], be).tobytes())
+    idx = np.arange(n, dtype=">u2" if n <= 65535 else ">i4").tobytes()
+    return head + pts.tobytes() + prim + idx + np.array([0], be).tobytes() + b"\x00\xff"
+
+
+class HoudiniFileSaver:
+    """houdini_file_saver (libclsph/file_save_delegates/houdini_file_saver.h:8-20).
+
+    `binary_bgeo` (default False) selects the binary .bgeo frame that the
+    reference writes when built with USE_PARTIO."""
+
+    def __init__(self, frames_folder_prefix: str, binary_bgeo: bool = False):
         self.frames_folder_prefix = frames_folder_prefix
+        self.binary_bgeo = binary_bgeo
         self.frame_count = 0
 
     def writeFrameToFile(self, particles: np.ndarray, parameters) -> int:
         self.frame_count += 1
-        name = f"{self.frames_folder_prefix}frames/frame{str(self.frame_count).zfill(9)[-7:]}.geo"
+        stem = f"{self.frames_folder_prefix}frames/frame{str(self.frame_count).zfill(9)[-7:]}"
+        if self.binary_bgeo:
+            try:
+                Path(stem + ".bgeo").write_bytes(bgeo_bytes(particles, parameters))
+            except OSError:
+                import sys
+
+                sys.stderr.write(f"Error while writing to {stem}.bgeo\n")
+            return 0
+        name = stem + ".geo"
         n = int(parameters["particles_count"])
         mass = _g(parameters["particle_mass"])
         lines = ["PGEOMETRY V5", f"NPoints {n} NPrims 1", "NPointGroups 0 NPrimGroups 1",
