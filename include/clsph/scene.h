@@ -15,6 +15,10 @@ class scene {
   std::vector<float> face_normals;
   std::vector<float> vertices;
   std::vector<unsigned int> indices;
+  // false (default): the reference's behaviour for files with several shapes
+  // (the mesh is the last shape's; face_normals holds every shape's normals).
+  // true: all shapes are concatenated into one mesh.
+  bool fix_multi_shape = false;
 };
 
 #endif

@@ -52,6 +52,11 @@ int clsph_host_scene_load(void* s, const char* filename) {
   return static_cast<scene*>(s)->load(filename) ? 1 : 0;
 }
 
+// scene::fix_multi_shape (0: the reference's behaviour, 1: shapes concatenated).
+void clsph_host_scene_set_fix_multi_shape(void* s, int on) {
+  static_cast<scene*>(s)->fix_multi_shape = on != 0;
+}
+
 void clsph_host_scene_sizes(void* s, uint32_t* face_count, uint64_t* normals, uint64_t* vertices,
                             uint64_t* indices) {
   scene* sc = static_cast<scene*>(s);

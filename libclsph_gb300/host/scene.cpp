@@ -161,6 +161,15 @@ bool scene::load(std::string filename) {
   }
   std::cout << "Scene Loading - number of shapes in file [" << filename << "]: " << shapes.size()
             << std::endl;
+  if (fix_multi_shape && !shapes.empty()) {
+    Shape all;
+    for (const Shape& s : shapes) {
+      const unsigned int base = (unsigned int)(all.positions.size() / 3);
+      for (unsigned int i : s.indices) all.indices.push_back(i + base);
+      all.positions.insert(all.positions.end(), s.positions.begin(), s.positions.end());
+    }
+    shapes.assign(1, all);
+  }
   for (const Shape& s : shapes) {
     indices = s.indices;
     if (indices.size() % 3 != 0) {

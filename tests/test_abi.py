@@ -57,6 +57,7 @@ def test_host_library_exports():
     lib = ctypes.CDLL(str(HOST_SO))
     for n in ("clsph_host_load_settings", "clsph_host_scene_new", "clsph_host_scene_load",
               "clsph_host_scene_sizes", "clsph_host_scene_copy", "clsph_host_scene_free",
+              "clsph_host_scene_set_fix_multi_shape",
               "clsph_host_write_houdini", "clsph_host_write_bgeo", "clsph_host_simulate", "clsph_host_last_error"):
         assert hasattr(lib, n), n
 

@@ -40,6 +40,7 @@ def host():
         [ctypes.POINTER(ctypes.c_uint64)] * 3
     lib.clsph_host_scene_copy.argtypes = [vp, vp, vp, vp]
     lib.clsph_host_scene_free.argtypes = [vp]
+    lib.clsph_host_scene_set_fix_multi_shape.argtypes = [vp, ctypes.c_int]
     lib.clsph_host_write_houdini.argtypes = [ctypes.c_char_p, vp, vp]
     return lib
 
@@ -168,6 +169,40 @@ def test_obj_reader_python_and_cpp_agree(tmp_path, host, name, monkeypatch):
     assert fc == py.face_count
     assert np.array_equal(idx, py.indices)
     assert np.array_equal(verts, py.vertices)
+    assert np.array_equal(normals.view(np.uint32), py.face_normals.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["shapes.obj", "quad_fan.obj"])
+def test_fix_multi_shape_python_and_cpp_agree(tmp_path, host, name, monkeypatch):
+    """With fix_multi_shape every shape's faces form one mesh (scene.cpp:23-33
+    keeps only the last shape's); one-shape files are unchanged."""
+    scenes = tmp_path / "scenes"
+    scenes.mkdir()
+    (scenes / name).write_text(OBJ_CASES[name])
+    monkeypatch.chdir(tmp_path)
+    py = Scene()
+    assert py.load(name, fix_multi_shape=True)
+    s = host.clsph_host_scene_new()
+    host.clsph_host_scene_set_fix_multi_shape(s, 1)
+    assert host.clsph_host_scene_load(s, name.encode()) == 1
+    fc = ctypes.c_uint32()
+    nn, nv, ni = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    host.clsph_host_scene_sizes(s, ctypes.byref(fc), ctypes.byref(nn), ctypes.byref(nv),
+                                ctypes.byref(ni))
+    normals = np.zeros(nn.value, np.float32)
+    verts = np.zeros(nv.value, np.float32)
+    idx = np.zeros(ni.value, np.uint32)
+    host.clsph_host_scene_copy(s, normals.ctypes.data, verts.ctypes.data, idx.ctypes.data)
+    host.clsph_host_scene_free(s)
+    faces = sum(1 for line in OBJ_CASES[name].splitlines() if line.startswith("f "))
+    if name == "quad_fan.obj":
+        faces = 3  # one pentagon, fanned
+        plain = Scene()
+        assert plain.load(name)
+        assert np.array_equal(plain.indices, py.indices)
+    assert fc.value == py.face_count == faces
+    assert len(normals) == 3 * faces
+    assert np.array_equal(idx, py.indices) and np.array_equal(verts, py.vertices)
     assert np.array_equal(normals.view(np.uint32), py.face_normals.view(np.uint32))
 
 
