@@ -9,7 +9,7 @@ the stable-sort permutation, the dense cell table, the AoS after the sort,
 after density_pressure, after forces, and after advection_collision.
 
 Run in the development container (needs the reference sources):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture name ...]
 """
 
 from __future__ import annotations
@@ -109,16 +109,57 @@ def case_trajectory():
             W.box_mesh((0, 0, 0), (1, 1, 1)), 5)
 
 
-CASES = [case_default_lattice, case_box_floor, case_mucus_corner, case_coincident, case_trajectory]
+def case_edge_hits():
+    """Particles whose path crosses a mesh edge or vertex exactly in this
+    substep, with no gravity and no neighbours, so each moves in a straight
+    line: onto the diagonal shared by the two triangles of the z = 0 face
+    (x == y there), onto the edges where two faces meet, and into the corners
+    where three meet. The hit distances tie between faces, which is where
+    "equal distance: the later face wins" decides the response. An interior
+    lattice spaced wider than h fills the scene to 216 particles."""
+    st = settings(216, constant_acceleration={"x": 0, "y": 0, "z": 0})
+    h = float(st.params["h"])
+    assert 0.1 > h
+    pos, vel = [], []
+    for t in np.arange(0.15, 0.9, 0.1, dtype=np.float32):  # the face diagonal
+        pos.append((t, t, 0.002))
+        vel.append((0.0, 0.0, -3.0))
+    for t in (0.25, 0.55, 0.85):  # edges between two faces
+        pos.append((0.002, t, 0.002))
+        vel.append((-2.0, 0.0, -2.0))
+        pos.append((t, 0.998, 0.002))
+        vel.append((0.0, 2.0, -2.0))
+    for c in [(0.003, 0.003, 0.003), (0.997, 0.003, 0.003), (0.003, 0.997, 0.997),
+              (0.997, 0.997, 0.997)]:  # corners
+        pos.append(c)
+        vel.append(tuple(-2.5 if x < 0.5 else 2.5 for x in c))
+    rng = np.random.default_rng(15)
+    need = 216 - len(pos)
+    fill = W.lattice((6, 6, 6), 0.1, (0.2, 0.2, 0.2), 0.0, rng)[:need]
+    pos = np.concatenate([np.array(pos, np.float32), fill.astype(np.float32)])
+    vel = np.concatenate([np.array(vel, np.float32),
+                          rng.normal(0, 0.2, (need, 3)).astype(np.float32)])
+    return ("edge_hits_216", st, particles_from_arrays(pos, vel, vel),
+            W.box_mesh((0, 0, 0), (1, 1, 1)), 1)
+
+
+CASES = [case_default_lattice, case_box_floor, case_mucus_corner, case_coincident, case_trajectory,
+         case_edge_hits]
 
 
 def main() -> None:
+    """Writes every fixture, or only those named on the command line (the
+    others keep their files and manifest entries)."""
     if build_ref() is None:
         raise SystemExit("reference sources not found; fixtures are generated in the dev container")
+    only = set(sys.argv[1:])
     ref = RefBuild()
-    manifest = {}
+    mpath = HERE / "manifest.json"
+    manifest = json.loads(mpath.read_text()) if only and mpath.exists() else {}
     for make in CASES:
         name, st, parts, mesh, steps = make()
+        if only and name not in only:
+            continue
         out = {"params": np.array(st.params).reshape(1), "terms": np.array(st.terms).reshape(1),
                "particles": parts, "vertices": mesh["vertices"], "indices": mesh["indices"],
                "face_normals": mesh["face_normals"], "steps": np.array([steps])}
@@ -136,7 +177,7 @@ def main() -> None:
         manifest[name] = {"n": int(len(parts)), "steps": steps,
                           "faces": int(len(mesh["indices"]) // 3)}
         print(name, manifest[name])
-    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    mpath.write_text(json.dumps(manifest, indent=1) + "\n")
 
 
 if __name__ == "__main__":
