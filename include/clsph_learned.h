@@ -140,10 +140,11 @@ int clsph_gpu_read_features(clsph_gpu* h, float* features_host);
 typedef struct {
   uint32_t dt_mult;  /* plain time steps per learned step (4) */
   float threshold;   /* rollback when the predicted density deviation exceeds this (0.01) */
-  uint32_t flags;    /* CLSPH_LEARNED_CALIBRATE: calibrate the check on fallback intervals */
+  uint32_t flags;    /* CLSPH_LEARNED_CALIBRATE: calibrate the check on fallback intervals;
+                        CLSPH_LEARNED_NO_CHECK: no density check (threshold ignored) */
 } clsph_learned_config;
 
-enum { CLSPH_LEARNED_CALIBRATE = 1 };
+enum { CLSPH_LEARNED_CALIBRATE = 1, CLSPH_LEARNED_NO_CHECK = 2 };
 
 typedef struct {
   uint64_t learned_steps;  /* accepted learned steps */
@@ -164,8 +165,10 @@ typedef struct {
  * check: the plain statistics it reaches, minus those the network predicted
  * for it, update an exponential average b (weight 0.3) that is added to
  * D_pred and M_pred of later checks (the calibration belongs to the handle
- * and restarts when another network is passed). stats (may be NULL) is
- * accumulated, not cleared. */
+ * and restarts when another network is passed). With CLSPH_LEARNED_NO_CHECK
+ * the learned steps run back to back with no check, snapshot or host wait
+ * (a diverging step is not caught; the call synchronises once at the end).
+ * stats (may be NULL) is accumulated, not cleared. */
 int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const clsph_learned_config* cfg,
                            clsph_learned_stats* stats);
 

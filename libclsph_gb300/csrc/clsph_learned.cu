@@ -1138,6 +1138,28 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
     L->rejected_m = g.m_pred;
     return 0;
   };
+  if (cfg->flags & CLSPH_LEARNED_NO_CHECK) {
+    // back to back on the stream: no snapshot, no gate, no host wait per step
+    for (uint32_t k = 0; k < steps; ++k) {
+      if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
+      if ((rc = enqueue_learned_tail(h, m, L, mult))) return rc;
+      ++h->substeps;
+    }
+    // the MLP kernel's error word, read once for the whole run
+    CUDA_TRY(cudaMemcpyAsync(L->dev_host + kGateSums, L->dev_sum + kGateSums, sizeof(float),
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    uint32_t errw;
+    std::memcpy(&errw, L->dev_host + kGateSums, sizeof(errw));
+    if (errw) return fail(CLSPH_ERR_CUDA, "step_learned: a tensor-core wait of the MLP kernel timed out");
+    h->have_fields = false;
+    if (stats) {
+      stats->learned_steps += steps;
+      stats->calibration_d = L->bias_d;
+      stats->calibration_m = L->bias_m;
+    }
+    return check_launch(h);
+  }
   int cur = 0;
   bool pending = false;  // the last learned step awaits its density check; its input is snap[cur ^ 1]
   uint32_t done = 0;

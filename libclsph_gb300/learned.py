@@ -52,6 +52,7 @@ class TrainConfig(ctypes.Structure):
 
 
 CALIBRATE = 1  # CLSPH_LEARNED_CALIBRATE
+NO_CHECK = 2  # CLSPH_LEARNED_NO_CHECK
 
 
 class LearnedConfig(ctypes.Structure):
@@ -268,10 +269,13 @@ def read_features(solver: GpuSolver) -> np.ndarray:
 
 
 def step_learned(solver: GpuSolver, mlp: Mlp, steps: int, dt_mult: int = 4, threshold: float = 0.01,
-                 stats: LearnedStats | None = None, calibrate: bool = False) -> LearnedStats:
+                 stats: LearnedStats | None = None, calibrate: bool = False,
+                 check: bool = True) -> LearnedStats:
+    """clsph_gpu_step_learned; check=False runs the steps back to back without
+    the density check (threshold ignored)."""
     lib = library()
     st = stats if stats is not None else LearnedStats()
-    cfg = LearnedConfig(dt_mult, threshold, CALIBRATE if calibrate else 0)
+    cfg = LearnedConfig(dt_mult, threshold, (CALIBRATE if calibrate else 0) | (0 if check else NO_CHECK))
     _check(lib, "clsph_gpu_step_learned",
            lib.clsph_gpu_step_learned(solver.h, mlp.h, steps, ctypes.byref(cfg), ctypes.byref(st)))
     return st

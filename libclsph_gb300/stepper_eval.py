@@ -72,7 +72,7 @@ def compare(p_state, p_rho, l_state, l_rho, params) -> dict:
 
 
 def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, checkpoints: int = 10,
-             threshold: float = 0.01, graph: bool = True) -> dict:
+             threshold: float = 0.01, graph: bool = True, check: bool = True) -> dict:
     import torch
 
     if plain_substeps % (dt_mult * checkpoints):
@@ -103,7 +103,7 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         stats = Lm.LearnedStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Lm.step_learned(lr, mlp, learned_steps, dt_mult, threshold, stats)
+        Lm.step_learned(lr, mlp, learned_steps, dt_mult, threshold, stats, check=check)
         lr.sync()
         learned_s = time.perf_counter() - t0
     # ---- accuracy: the same trajectories with checkpoints
@@ -117,7 +117,7 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         for c in range(checkpoints):
             p.step(per)
             pc.step(per)
-            Lm.step_learned(lr, mlp, per // dt_mult, dt_mult, threshold, chk_stats)
+            Lm.step_learned(lr, mlp, per // dt_mult, dt_mult, threshold, chk_stats, check=check)
             ps, prho = by_id(p, scratch)
             ls, lrho = by_id(lr, scratch)
             cs, crho = by_id(pc, scratch)
@@ -132,7 +132,7 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         "workload": scene.name,
         "particles": scene.n,
         "dt_mult": dt_mult,
-        "threshold": threshold,
+        "threshold": threshold if check else None,
         "plain_substeps": plain_substeps,
         "learned_steps": learned_steps,
         "sim_time_s": sim_time,

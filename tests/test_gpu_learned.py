@@ -321,6 +321,24 @@ def test_collector_keeps_trajectory_and_targets(gpu_lib):
     assert close.mean() > 0.9, close.mean()
 
 
+def test_no_check_run_equals_unlimited_check(gpu_lib):
+    """check=False (no snapshots, gates or host waits) advances the state
+    exactly as a check that never fires."""
+    sc = W.small_block(12, seed=9, velocity_sigma=0.3, offset=(0.2, 0.05, 0.2))
+    m = Lm.Mlp(blob=random_blob(4, scale=0.05))
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as a, GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as b:
+        a.upload(sc.particles)
+        b.upload(sc.particles)
+        sa = Lm.step_learned(a, m, 5, threshold=1e30)
+        sb = Lm.step_learned(b, m, 5, check=False)
+        pa, pb = a.download(), b.download()
+    assert sa.learned_steps == sb.learned_steps == 5
+    assert sb.checks == 0 and sb.rejected == 0
+    for f in ("position", "velocity", "intermediate_velocity"):
+        assert np.array_equal(pa[f][:, :3], pb[f][:, :3]), f
+    m.close()
+
+
 def test_collector_on_learned_rollout(gpu_lib):
     """Sampling along learned steps leaves the learned trajectory unchanged and
     yields one sample per tracked particle per learned step."""
