@@ -1,0 +1,45 @@
+"""bench.py on a machine without a GPU: the reference arm (the oracle on the
+host cores) prints its one JSON line with the keys of the bench contract, and
+the GPU arm stops with an error instead of falling back to the CPU."""
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def run_bench(*args):
+    return subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], capture_output=True,
+                          text=True, cwd=ROOT, timeout=900)
+
+
+def test_reference_arm_line():
+    r = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--workload",
+                  "dam_break_32k")
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == d["unit"] == "particle-steps/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["steps"] == 1 and d["warmup"] >= 3  # at least 3 warm-up steps, whatever is asked
+    assert d["config"]["workload"] == "dam_break_32768"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+def test_gpu_arm_fails_without_a_device():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    r = run_bench("--steps", "1", "--warmup", "3", "--workload", "dam_break_32k")
+    assert r.returncode != 0
+    assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
