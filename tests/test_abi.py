@@ -53,6 +53,15 @@ def test_gpu_library_exports_learned_symbols():
     assert lib.clsph_mlp_blob_size() == BLOB == 75268 + 72
 
 
+def test_learned_flags_match_header():
+    text = (ROOT / "include" / "clsph_learned.h").read_text()
+    flags = dict((k, int(v)) for k, v in re.findall(r"(CLSPH_LEARNED_\w+)\s*=\s*(\d+)", text))
+    from libclsph_gb300 import learned
+
+    assert flags == {"CLSPH_LEARNED_CALIBRATE": learned.CALIBRATE,
+                     "CLSPH_LEARNED_NO_CHECK": learned.NO_CHECK}
+
+
 def test_host_library_exports():
     lib = ctypes.CDLL(str(HOST_SO))
     for n in ("clsph_host_load_settings", "clsph_host_scene_new", "clsph_host_scene_load",
