@@ -159,6 +159,7 @@ struct clsph_gpu {
   cudaGraphExec_t graph_exec[2][2] = {};
   uint32_t graph_max_iters[2][2] = {};
   uint64_t graph_launches[2][2] = {};  // kernels in one replay of each graph
+  uint32_t graph_epoch = 0;  // counts drop_graph(): other cached graphs compare it
 
   // buffers of the learned stepper (clsph_learned.cu), made on first use
   void* learned = nullptr;
@@ -218,6 +219,7 @@ struct clsph_gpu {
   }
 
   void drop_graph() {
+    ++graph_epoch;
     for (auto& row : graph_exec)
       for (auto& g : row) {
         if (g) cudaGraphExecDestroy(g);

@@ -14,6 +14,7 @@
 // prediction to accept the step or roll it back.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -318,6 +319,7 @@ struct clsph_mlp {
   bf16* w1b = nullptr;    // [32][256]
   bf16* w2b = nullptr;    // [256][256]
   bf16* w3b = nullptr;    // [256][8]
+  uint64_t serial = 0;    // unique per network made in this process (keys cached graphs)
   bf16* w1t = nullptr;    // [256][32]
   bf16* w2t = nullptr;    // [256][256]
   bf16* w3t = nullptr;    // [16][256]
@@ -510,6 +512,13 @@ struct LearnedCache {
   double bias_d = 0.0, bias_m = 0.0;
   bool calib_pending = false;        // a fallback interval awaits its plain statistics
   double rejected_d = 0.0, rejected_m = 0.0;  // predictions for that interval
+  // unchecked learned steps replayed from a CUDA graph, one per buffer the
+  // particle ids start in; rebuilt when the network, dt_mult, the collision
+  // cap or the handle's launch shapes (graph_epoch) change
+  cudaGraphExec_t nc_graph[2] = {};
+  uint64_t nc_mlp[2] = {};
+  uint32_t nc_mult[2] = {}, nc_max_iters[2] = {}, nc_epoch[2] = {};
+  uint64_t nc_launches[2] = {};  // kernels in one replay
 };
 
 void free_cache(clsph_gpu* h) {
@@ -527,6 +536,8 @@ void free_cache(clsph_gpu* h) {
   cudaFree(L->dev_sum);
   if (L->dev_host) cudaFreeHost(L->dev_host);
   if (L->ev) cudaEventDestroy(L->ev);
+  for (auto& g : L->nc_graph)
+    if (g) cudaGraphExecDestroy(g);
   delete L;
   h->learned = nullptr;
 }
@@ -657,6 +668,50 @@ int plain_substeps(clsph_gpu* h, uint32_t count) {
   return 0;
 }
 
+// An even number of unchecked learned steps (density pass + learned tail),
+// captured once and replayed like the plain substeps' graphs. The particle
+// ids alternate between their two buffers once per step, so an even count
+// returns them to the buffer it started from; one graph per starting buffer.
+constexpr uint32_t kLearnedGraphLen = 4;
+
+int ensure_nocheck_graph(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t mult) {
+  const int par = h->ids_sel;
+  cudaGraphExec_t& ge = L->nc_graph[par];
+  if (ge && L->nc_mlp[par] == m->serial && L->nc_mult[par] == mult && L->nc_max_iters[par] == h->max_iters &&
+      L->nc_epoch[par] == h->graph_epoch)
+    return 0;
+  if (ge) cudaGraphExecDestroy(ge);
+  ge = nullptr;
+  cudaGraph_t graph = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const uint64_t launches = h->launches;
+  int rc = 0;
+  for (uint32_t k = 0; k < kLearnedGraphLen && !rc; ++k) {
+    rc = enqueue_substep(h, CLSPH_STAGE_DENSITY);
+    if (!rc) rc = enqueue_learned_tail(h, m, L, mult);
+  }
+  L->nc_launches[par] = h->launches - launches;
+  h->launches = launches;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("learned graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&ge, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    ge = nullptr;
+    return fail(CLSPH_ERR_CUDA, std::string("learned graph instantiate: ") + cudaGetErrorString(e));
+  }
+  if (h->ids_sel != par) return fail(CLSPH_ERR_STATE, "learned graph: particle ids did not return to their buffer");
+  L->nc_mlp[par] = m->serial;
+  L->nc_mult[par] = mult;
+  L->nc_max_iters[par] = h->max_iters;
+  L->nc_epoch[par] = h->graph_epoch;
+  return 0;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -698,6 +753,8 @@ int clsph_mlp_create(uint64_t seed, clsph_mlp** out) {
   if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
     return fail(CLSPH_ERR_NO_DEVICE, "mlp_create: no CUDA device");
   auto* m = new clsph_mlp();
+  static std::atomic<uint64_t> next_serial{1};
+  m->serial = next_serial++;
   cudaGetDevice(&m->device);
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device) == cudaSuccess && sms > 0)
@@ -1139,8 +1196,19 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
     return 0;
   };
   if (cfg->flags & CLSPH_LEARNED_NO_CHECK) {
-    // back to back on the stream: no snapshot, no gate, no host wait per step
-    for (uint32_t k = 0; k < steps; ++k) {
+    // back to back on the stream: no snapshot, no gate, no host wait per step;
+    // groups of kLearnedGraphLen steps replay one CUDA graph when the handle
+    // uses graphs
+    uint32_t k = 0;
+    if (h->use_graph && !h->profiling && steps >= kLearnedGraphLen) {
+      if ((rc = ensure_nocheck_graph(h, m, L, mult))) return rc;
+      for (; k + kLearnedGraphLen <= steps; k += kLearnedGraphLen) {
+        CUDA_TRY(cudaGraphLaunch(L->nc_graph[h->ids_sel], h->stream));
+        h->launches += L->nc_launches[h->ids_sel];
+        h->substeps += kLearnedGraphLen;
+      }
+    }
+    for (; k < steps; ++k) {
       if ((rc = enqueue_substep(h, CLSPH_STAGE_DENSITY))) return rc;
       if ((rc = enqueue_learned_tail(h, m, L, mult))) return rc;
       ++h->substeps;

@@ -100,6 +100,7 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
         p.sync()
         plain_s = time.perf_counter() - t0
     with solver() as lr:
+        lr.set_graph(graph)
         stats = Lm.LearnedStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -111,6 +112,7 @@ def evaluate(scene, mlp: Lm.Mlp, plain_substeps: int = 2000, dt_mult: int = 4, c
     with solver() as p, solver() as lr, solver() as scratch, solver(perturbed) as pc:
         p.set_graph(graph)
         pc.set_graph(graph)
+        lr.set_graph(graph)
         chk_stats = Lm.LearnedStats()
         per = plain_substeps // checkpoints
         h = float(scene.params["h"])

@@ -323,20 +323,35 @@ def test_collector_keeps_trajectory_and_targets(gpu_lib):
 
 def test_no_check_run_equals_unlimited_check(gpu_lib):
     """check=False (no snapshots, gates or host waits) advances the state
-    exactly as a check that never fires."""
+    exactly as a check that never fires, launched step by step and replayed
+    from CUDA graphs of 4 steps (9 steps: two replays and one launched step;
+    then 4 more with another network, which rebuilds the graph)."""
     sc = W.small_block(12, seed=9, velocity_sigma=0.3, offset=(0.2, 0.05, 0.2))
     m = Lm.Mlp(blob=random_blob(4, scale=0.05))
-    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as a, GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as b:
-        a.upload(sc.particles)
-        b.upload(sc.particles)
-        sa = Lm.step_learned(a, m, 5, threshold=1e30)
-        sb = Lm.step_learned(b, m, 5, check=False)
-        pa, pb = a.download(), b.download()
-    assert sa.learned_steps == sb.learned_steps == 5
+    m2 = Lm.Mlp(blob=random_blob(5, scale=0.05))
+    solvers = [GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) for _ in range(3)]
+    try:
+        a, b, c = solvers
+        for s in solvers:
+            s.upload(sc.particles)
+        c.set_graph(True)
+        sa = Lm.step_learned(a, m, 9, threshold=1e30)
+        sb = Lm.step_learned(b, m, 9, check=False)
+        sc_ = Lm.step_learned(c, m, 9, check=False)
+        for s in solvers[1:]:
+            Lm.step_learned(s, m2, 4, check=False)
+        Lm.step_learned(a, m2, 4, threshold=1e30)
+        pa, pb, pc = (s.download() for s in solvers)
+    finally:
+        for s in solvers:
+            s.close()
+    assert sa.learned_steps == sb.learned_steps == sc_.learned_steps == 9
     assert sb.checks == 0 and sb.rejected == 0
     for f in ("position", "velocity", "intermediate_velocity"):
         assert np.array_equal(pa[f][:, :3], pb[f][:, :3]), f
+        assert np.array_equal(pa[f][:, :3], pc[f][:, :3]), f
     m.close()
+    m2.close()
 
 
 def test_collector_on_learned_rollout(gpu_lib):
