@@ -216,6 +216,24 @@ enum {
 };
 int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode);
 
+/* Bounds of the engine's device-side waits; no counterpart in the reference,
+ * whose OpenCL queue has no device-side waits. radix_lookback_spins bounds
+ * each radix-sort look-back wait (default CLSPH_DEFAULT_LOOKBACK_SPINS): a
+ * wait that runs out leaves that substep's order wrong, keeps every access in
+ * bounds and makes the next clsph_gpu_sync return CLSPH_ERR_CUDA.
+ * mlp_wait_polls bounds each mbarrier wait of the learned stepper's tcgen05
+ * MLP kernel (default CLSPH_DEFAULT_MLP_WAIT_POLLS; 0 gives up at once): a wait
+ * that runs out makes clsph_gpu_step_learned return CLSPH_ERR_CUDA.
+ * radix_withheld_tile (CLSPH_NO_TILE in normal use) is a test hook of the
+ * failure path: that tile of every radix pass never publishes its digit
+ * counts, so the tile after it waits on a word nothing sets until its bound
+ * runs out. Takes effect at the next launch (cached graphs are rebuilt). */
+#define CLSPH_DEFAULT_LOOKBACK_SPINS (1u << 20)
+#define CLSPH_DEFAULT_MLP_WAIT_POLLS (1u << 24)
+#define CLSPH_NO_TILE 0xFFFFFFFFu
+int clsph_gpu_set_wait_limits(clsph_gpu* h, uint32_t radix_lookback_spins, uint32_t mlp_wait_polls,
+                              uint32_t radix_withheld_tile);
+
 /* Counters since create: [0] substeps, [1] particles whose collision loop hit
  * the cap, [2] kernel launches. */
 int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3);
@@ -233,7 +251,10 @@ int clsph_gpu_counters(clsph_gpu* h, uint64_t* out3);
  * CLSPH_ERR_TOO_LARGE. All calls share that array (each clears what must
  * start at zero): calls whose GPU work overlaps race, so serialise them. The
  * first call on a device looks the array up (cudaGetSymbolAddress) with that
- * device current; make it before any stream capture. Asynchronous on
+ * device current; make it before any stream capture. The address is kept for
+ * the life of the process: after cudaDeviceReset the device's code is loaded
+ * anew and that address is stale, so a process that resets a device must not
+ * call this function on it again. Asynchronous on
  * `cuda_stream` (a cudaStream_t, NULL = legacy default stream). */
 int clsph_gpu_sort_keys_noalloc(const uint32_t* keys_in, uint32_t* keys_out, uint32_t* perm_out,
                                 uint32_t n, void* cuda_stream);

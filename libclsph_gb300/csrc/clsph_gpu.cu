@@ -24,6 +24,8 @@ static_assert(offsetof(clsph_parameters, constant_acceleration) == 64, "paramete
 static_assert(offsetof(clsph_parameters, grid_size_x) == 80, "parameter layout");
 static_assert(offsetof(clsph_parameters, min_point) == 96, "parameter layout");
 static_assert(sizeof(clsph_kernel_terms) == 20, "kernel constant layout");
+static_assert(kRadixLookbackSpins == CLSPH_DEFAULT_LOOKBACK_SPINS, "default look-back bound");
+static_assert(kNoTile == CLSPH_NO_TILE, "withheld-tile sentinel");
 
 namespace clsph_host {
 
@@ -91,7 +93,8 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   for (int pass = 0; pass < 4; ++pass)
     h->launch(K_RADIX_SWEEP, k_radix_onesweep, dim3(h->ntiles), dim3(kRadixThreads), h->keys, h->vals, n,
               pass, cctl, (const uint32_t*)h->digit_total, h->lookback, h->ntiles,
-              h->step_counters + kCntRadixTile + pass, h->status);
+              h->step_counters + kCntRadixTile + pass, h->status, h->radix_spin_limit,
+              h->radix_withheld_tile);
   const int src_ids = h->ids_sel, dst_ids = h->ids_sel ^ 1;
   h->launch(K_GATHER, k_gather, dim3(blocks), dim3(kBlock), n, (const DevGrid*)h->grids,
             (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
@@ -401,6 +404,8 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
       cudaMemset(h->capped, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemset(h->aux, 0, sizeof(float4) * n) != cudaSuccess ||
       cudaMemset(h->ncount, 0, sizeof(uint32_t) * n) != cudaSuccess ||
+      cudaMemset(h->keys, 0, sizeof(uint32_t) * 2 * (size_t)n) != cudaSuccess ||
+      cudaMemset(h->vals, 0, sizeof(uint32_t) * 2 * (size_t)n) != cudaSuccess ||
       cudaMemset(h->acc, 0, sizeof(float4) * n) != cudaSuccess ||
       cudaMemcpy(h->ctl, ctl_init, sizeof(ctl_init), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(h->scene_of, scene_of.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -844,6 +849,17 @@ int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode) {
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   h->search = mode;
   h->drop_graph();
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_wait_limits(clsph_gpu* h, uint32_t radix_lookback_spins, uint32_t mlp_wait_polls,
+                              uint32_t radix_withheld_tile) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_wait_limits: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->radix_spin_limit = radix_lookback_spins;
+  h->mlp_wait_limit = mlp_wait_polls;
+  h->radix_withheld_tile = radix_withheld_tile;
+  h->drop_graph();  // the limits are kernel arguments of the captured launches
   return CLSPH_OK;
 }
 

@@ -145,6 +145,11 @@ struct clsph_gpu {
   int forces_block = 128;
   uint32_t advect_blocks_per_sm = 8;
 
+  // bounds of the device waits (clsph_gpu_set_wait_limits)
+  uint32_t radix_spin_limit = CLSPH_DEFAULT_LOOKBACK_SPINS;
+  uint32_t radix_withheld_tile = CLSPH_NO_TILE;
+  uint32_t mlp_wait_limit = CLSPH_DEFAULT_MLP_WAIT_POLLS;
+
   bool uploaded = false;
   bool partial = false;
   bool have_fields = false;

@@ -414,10 +414,18 @@ static __global__ void __launch_bounds__(kBlock)
 // all tiles up to it), bits 0-29 the value (n < 2^28). Tiles are numbered in
 // the order blocks start (an atomic ticket), so every tile a block waits for
 // belongs to a block that is already running and publishes without waiting
-// itself; the wait is bounded all the same (kRadixLookbackSpins), and a wait
-// that runs out raises kFlagSortStall, which clsph_gpu_sync reports as an
-// error.
+// itself; the wait is bounded all the same (spin_limit, by default
+// kRadixLookbackSpins), and a wait that runs out raises kFlagSortStall, which
+// clsph_gpu_sync reports as an error. After a stall the offsets of the tiles
+// behind it are wrong, but every store stays in bounds (destinations >= n are
+// skipped, and the slots a pass leaves unwritten keep earlier in-range
+// values), so the context stays usable.
+//
+// withheld_tile (a test hook of clsph_gpu_set_wait_limits; kNoTile in normal
+// use): that tile never publishes its words, so the tile after it waits on a
+// word that nothing sets until its spin limit runs out.
 constexpr uint32_t kRadixLookbackSpins = 1u << 20;
+constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 constexpr uint32_t kLbAggregate = 1u << 30, kLbInclusive = 2u << 30, kLbValue = (1u << 30) - 1u;
 
 __device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* p) {
@@ -465,7 +473,7 @@ static __global__ void __launch_bounds__(kRadixThreads)
     k_radix_onesweep(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
                      int pass, const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ digit_total,
                      uint32_t* __restrict__ lookback, uint32_t ntiles, uint32_t* __restrict__ tile_ticket,
-                     uint32_t* __restrict__ status) {
+                     uint32_t* __restrict__ status, uint32_t spin_limit, uint32_t withheld_tile) {
   if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
   __shared__ uint32_t cnt[kRadixWarps][256];
   __shared__ uint32_t hist[256];
@@ -500,7 +508,8 @@ static __global__ void __launch_bounds__(kRadixThreads)
   const uint32_t d = threadIdx.x;  // this thread's digit in the look-back and the offsets
   const uint32_t local = hist[d];  // the tile's count of digit d
   uint32_t* lb = lookback + (size_t)pass * ntiles * 256u;
-  st_relaxed_gpu(&lb[(size_t)tile * 256u + d], (tile == 0 ? kLbInclusive : kLbAggregate) | local);
+  const bool publish = tile != withheld_tile;
+  if (publish) st_relaxed_gpu(&lb[(size_t)tile * 256u + d], (tile == 0 ? kLbInclusive : kLbAggregate) | local);
   // ranks within the tile: per warp in key order (rows of 32), then warps in order
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
@@ -539,14 +548,14 @@ static __global__ void __launch_bounds__(kRadixThreads)
       }
       t -= used;
       if (!done && used == 0) {
-        if (++spins > kRadixLookbackSpins) {
+        if (++spins > spin_limit) {
           atomicOr(status, kFlagSortStall);
           break;
         }
         __nanosleep(32);
       }
     }
-    st_relaxed_gpu(&lb[(size_t)tile * 256u + d], kLbInclusive | (excl + local));
+    if (publish) st_relaxed_gpu(&lb[(size_t)tile * 256u + d], kLbInclusive | (excl + local));
   }
   __syncthreads();
   {  // per digit: exclusive prefix over warps
@@ -604,7 +613,7 @@ static __global__ void __launch_bounds__(kBlock)
   const uint32_t* perm = vals_base + (size_t)sel * n;
   bool first = false;
   if (s < n) {
-    const uint32_t from = perm[s];
+    const uint32_t from = min(perm[s], n - 1u);  // in range even after a flagged sort stall
     const uint32_t key = keys[s];
     float4 p = src.pos[from];
     p.w = __uint_as_float(half_code(p, split.morton(key), grids[scene_of[s]]));

@@ -255,10 +255,13 @@ int launch_infer(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows
   return 0;
 }
 
+static_assert(clsph_nn::kTcWaitLimit == CLSPH_DEFAULT_MLP_WAIT_POLLS, "default MLP wait bound");
+
 // tcgen05 inference; *err collects wait timeouts (see k_mlp_tc)
 template <class Store>
 int launch_tc(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows, const clsph_nn::TcWeights& w,
               Store store, uint32_t* err, clsph_gpu* h, int cls) {
+  const uint32_t wait_limit = h ? h->mlp_wait_limit : clsph_nn::kTcWaitLimit;
   cudaError_t e = cudaFuncSetAttribute(clsph_nn::k_mlp_tc<Store>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)clsph_nn::kTcSmem);
   if (e != cudaSuccess)
@@ -267,9 +270,10 @@ int launch_tc(cudaStream_t stream, uint32_t sms, const bf16* x, uint32_t rows, c
   const uint32_t blocks = std::max(1u, std::min(tiles, sms));
   if (h)
     h->launch_smem(cls, clsph_nn::k_mlp_tc<Store>, dim3(blocks), dim3(clsph_nn::kTcThreads), clsph_nn::kTcSmem,
-                   x, rows, w, store, err);
+                   x, rows, w, store, err, wait_limit);
   else
-    clsph_nn::k_mlp_tc<Store><<<blocks, clsph_nn::kTcThreads, clsph_nn::kTcSmem, stream>>>(x, rows, w, store, err);
+    clsph_nn::k_mlp_tc<Store><<<blocks, clsph_nn::kTcThreads, clsph_nn::kTcSmem, stream>>>(x, rows, w, store, err,
+                                                                                          wait_limit);
   return 0;
 }
 
@@ -564,7 +568,11 @@ int ensure_cache(clsph_gpu* h, LearnedCache** out) {
     if ((rc = dev_alloc(&s.pos, n)) || (rc = dev_alloc(&s.vel, n)) || (rc = dev_alloc(&s.ivel, n)) ||
         (rc = dev_alloc(&s.ids, n)) || (rc = dev_alloc(&s.bbox, 6 * (size_t)h->nscenes)))
       return bail(rc);
+  // the correction and feature rows start defined: a learned step whose MLP
+  // stopped early (a wait ran out, reported as an error) reads them as they are
   if (cudaMemset(L->dev_sum, 0, (kGateSums + 1) * sizeof(float)) != cudaSuccess ||
+      cudaMemset(L->corr, 0, sizeof(float4) * n) != cudaSuccess ||
+      cudaMemset(L->x, 0, sizeof(bf16) * n * kFeat) != cudaSuccess ||
       cudaMallocHost(reinterpret_cast<void**>(&L->dev_host), (kGateSums + 1) * sizeof(float)) != cudaSuccess ||
       cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(CLSPH_ERR_CUDA, "step_learned: buffer set-up"));
@@ -649,7 +657,7 @@ int enqueue_learned_tail(clsph_gpu* h, clsph_mlp* m, LearnedCache* L, uint32_t d
   int rc = launch_forces_hooked(h, fh);
   if (rc) return rc;
   rc = launch_tc(h->stream, h->sm_count, L->x, n, tc_weights(m), clsph_nn::StoreRaw{L->corr},
-                 reinterpret_cast<uint32_t*>(L->dev_sum + 1), h, K_MLP);
+                 reinterpret_cast<uint32_t*>(L->dev_sum + kGateSums), h, K_MLP);
   if (rc) return rc;
   h->launch(K_LEARNED_ADVECT, k_advect<true>, dim3(grid_blocks(n, h->sm_count * h->advect_blocks_per_sm)),
             dim3(kBlock), n, h->st[1], (const float4*)h->acc, h->st[0], (const DevMesh*)h->meshes,
@@ -1174,6 +1182,8 @@ int clsph_gpu_step_learned(clsph_gpu* h, clsph_mlp* m, uint32_t steps, const cls
     L->calib_pending = false;
   }
   CUDA_TRY(cudaStreamSynchronize(m->stream));  // weights in place
+  // the MLP kernel's error word collects this call's wait timeouts only
+  CUDA_TRY(cudaMemsetAsync(L->dev_sum + kGateSums, 0, sizeof(float), h->stream));
   const uint32_t mult = cfg->dt_mult;
   clsph_learned_stats st{};
   auto record = [&](const GateStats& g, double dev) {

@@ -23,6 +23,10 @@
 // gets one commit and one wait per tile, so a wait never meets a phase that
 // completed twice. Every wait is bounded; a wait that runs out sets *err, the
 // CTA leaves its tile loop, waits (bounded) for its own MMAs and frees TMEM.
+// The waits of the tile loop give up after `wait_limit` polls (by default
+// kTcWaitLimit; a test hook sets 0 to make one run out); the teardown's waits
+// for MMAs still in flight always allow kTcWaitLimit polls, so tensor memory
+// is never freed under a running MMA.
 //
 // Encodings (PTX ISA, tcgen05): shared-memory descriptor = start address >> 4
 // in bits 0-13, leading-dimension byte offset >> 4 in 16-29 (distance between
@@ -65,7 +69,7 @@ constexpr uint32_t kTcIdesc3 = tc_idesc(kTcRows, kOut3);
 // tensor-memory columns within a tile's 256-column region
 constexpr uint32_t kTcRegion = 256;
 constexpr uint32_t kTcAcc3 = 32;  // layer-3 accumulator: columns the packing leaves free
-constexpr uint32_t kTcWaitLimit = 1u << 24;
+constexpr uint32_t kTcWaitLimit = 1u << 24;  // = CLSPH_DEFAULT_MLP_WAIT_POLLS
 
 struct TcWeights {
   const bf16* w1t;  // [256][32]  (W1 transposed: output-major, K contiguous)
@@ -105,8 +109,8 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
                : "memory");
 }
 
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kTcWaitLimit; ++i) {
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -216,7 +220,8 @@ __device__ __forceinline__ uint32_t tc_h2_col(int ks) {
 
 template <class Store>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_mlp_tc(const bf16* __restrict__ x, uint32_t rows, TcWeights w, Store store, uint32_t* __restrict__ err) {
+    k_mlp_tc(const bf16* __restrict__ x, uint32_t rows, TcWeights w, Store store, uint32_t* __restrict__ err,
+             uint32_t wait_limit) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const uint32_t sb = smem_addr(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   };
   // a wait that runs out keeps its phase, so the teardown waits for the same one
   auto wait_on = [&](uint32_t b, uint32_t& ph, uint32_t& pending) {
-    const bool got = tc_wait(b, ph);
+    const bool got = tc_wait(b, ph, wait_limit);
     if (got) {
       ph ^= 1;
       if (tid == 0) --pending;
@@ -367,9 +372,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // commit tracks every MMA issued before it; each barrier's oldest unwaited
   // commit is the phase to wait for)
   if (tid == 0) {
-    if (n1 && !tc_wait(bar_l1, ph1)) atomicOr(err, 2u);
-    if (n2 && !tc_wait(bar_l2, ph2)) atomicOr(err, 2u);
-    if (n3 && !tc_wait(bar_l3, ph3)) atomicOr(err, 2u);
+    if (n1 && !tc_wait(bar_l1, ph1, kTcWaitLimit)) atomicOr(err, 2u);
+    if (n2 && !tc_wait(bar_l2, ph2, kTcWaitLimit)) atomicOr(err, 2u);
+    if (n3 && !tc_wait(bar_l3, ph3, kTcWaitLimit)) atomicOr(err, 2u);
   }
   if (!ok && tid == 0) atomicOr(err, 1u);
   tc_fence_before();

@@ -224,7 +224,10 @@ __global__ void __launch_bounds__(kThreads) k_na_scatter(Buffers b, uint32_t n, 
   }
 }
 
-// Device address of g_sort_scratch, looked up once per device.
+// Device address of g_sort_scratch, looked up once per device and kept for
+// the life of the process (a cudaDeviceReset reloads the device code and
+// makes it stale; the header tells callers not to use the entry point on a
+// device after resetting it).
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 uint32_t* g_scratch_addr[kMaxDevices] = {};

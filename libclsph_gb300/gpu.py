@@ -22,6 +22,8 @@ STAGE_GRID, STAGE_SORT, STAGE_DENSITY, STAGE_FORCES, STAGE_ADVECT = 1, 2, 3, 4, 
 SEARCH_WINDOW, SEARCH_CELL_WARPS, SEARCH_PARTICLE_WARPS = 0, 1, 2
 SEARCH_MODES = (SEARCH_WINDOW, SEARCH_CELL_WARPS, SEARCH_PARTICLE_WARPS)
 WARN_GRID_OVERFLOW, WARN_COLLISION_CAP, WARN_NONFINITE = 1, 2, 4
+# bounds of the device waits (clsph_gpu_set_wait_limits)
+DEFAULT_LOOKBACK_SPINS, DEFAULT_MLP_WAIT_POLLS, NO_TILE = 1 << 20, 1 << 24, 0xFFFFFFFF
 
 _vp = ctypes.c_void_p
 _u32 = ctypes.c_uint32
@@ -56,6 +58,7 @@ SIGNATURES = [
     ("clsph_gpu_autotune", ctypes.c_int, [_vp, _u32, ctypes.c_char_p, ctypes.c_int]),
     ("clsph_gpu_set_launch_shape", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u32]),
     ("clsph_gpu_set_neighbour_search", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("clsph_gpu_set_wait_limits", ctypes.c_int, [_vp, _u32, _u32, _u32]),
     ("clsph_gpu_last_error", ctypes.c_char_p, []),
 ]
 
@@ -276,6 +279,15 @@ class GpuSolver:
     def set_neighbour_search(self, mode: int) -> None:
         """SEARCH_WINDOW, SEARCH_CELL_WARPS or SEARCH_PARTICLE_WARPS (bit-identical results)."""
         _check("clsph_gpu_set_neighbour_search", self.lib.clsph_gpu_set_neighbour_search(self.h, mode))
+
+    def set_wait_limits(self, radix_lookback_spins: int = DEFAULT_LOOKBACK_SPINS,
+                        mlp_wait_polls: int = DEFAULT_MLP_WAIT_POLLS,
+                        radix_withheld_tile: int = NO_TILE) -> None:
+        """Bounds of the device-side waits; radix_withheld_tile is the test
+        hook that makes one look-back wait run out (see clsph_gpu.h)."""
+        _check("clsph_gpu_set_wait_limits",
+               self.lib.clsph_gpu_set_wait_limits(self.h, radix_lookback_spins, mlp_wait_polls,
+                                                  radix_withheld_tile))
 
     def counters(self) -> dict:
         c = np.zeros(3, dtype=np.uint64)

@@ -73,6 +73,37 @@ def test_noalloc_sort_at_its_maximum(gpu_lib):
     assert np.array_equal(got_keys, keys[want])
 
 
+def test_noalloc_sort_allocates_no_device_memory(gpu_lib):
+    """Free device memory is the same before and after two calls (the first
+    call, which loads the library's device code and its static array, comes
+    before the measurement; every buffer is allocated up front)."""
+    import torch
+
+    rng = np.random.default_rng(24)
+    n = MAX_KEYS
+    keys = rng.integers(0, 1 << 24, n, dtype=np.uint32)
+    dev_in = torch.from_numpy(keys.view(np.int32)).cuda()
+    dev_keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    dev_perm = torch.empty(n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = gpu_lib.clsph_gpu_sort_keys_noalloc(dev_in.data_ptr(), dev_keys.data_ptr(),
+                                                 dev_perm.data_ptr(), n, stream.cuda_stream)
+        assert rc == 0, gpu_lib.clsph_gpu_last_error()
+
+    call()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    call()
+    call()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    want = np.argsort(keys, kind="stable").astype(np.uint32)
+    assert np.array_equal(dev_perm.cpu().numpy().view(np.uint32), want)
+
+
 def test_noalloc_sort_rejects_oversize(gpu_lib):
     rc = gpu_lib.clsph_gpu_sort_keys_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16),
                                              ctypes.c_void_p(16), MAX_KEYS + 1, None)
