@@ -8,6 +8,12 @@
   break after a few substeps, and the 4,194,304-particle pour onto a
   131,072-triangle heightfield, whose collisions the oracle cannot run at
   that size).
+* Ten substeps of the 1M dam break against ten oracle substeps (chaotic in
+  the long run, but bit for bit over ten substeps).
+* The GPU's FP32 density, pressure and acceleration of the 1M dam break
+  reported against the FP64 oracle (the same algorithm in double): maximum
+  and mean relative error per field, bounded at 1e-5 (density), 1e-4
+  (pressure) and 1e-5 of the largest acceleration.
 * Size-independent properties after several substeps: keys non-decreasing,
   the sort permutation and the particle ids are permutations, the cell table
   is the lower bound of every cell in the sorted keys, no device flags.
@@ -49,6 +55,59 @@ def test_dam_break_1m_substep_matches_oracle(gpu_lib, oracle, dam_break):
     for f in ("position", "velocity", "intermediate_velocity"):
         assert np.array_equal(out[f][:, :3], ref.final[f][:, :3]), f
     assert np.array_equal(out["density"], ref.final["density"])
+
+
+def test_dam_break_1m_ten_substeps_match_oracle(gpu_lib, oracle, dam_break):
+    sc = dam_break
+    want = oracle.run(sc.params, sc.terms, sc.particles, 10, sc.mesh)
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.upload(sc.particles)
+        g.step(10)
+        assert g.sync() == 0
+        out = g.download()
+    for f in ("position", "velocity", "intermediate_velocity"):
+        assert np.array_equal(out[f][:, :3], want[f][:, :3]), f
+    assert np.array_equal(out["density"], want["density"])
+    assert np.array_equal(out["pressure"], want["pressure"])
+
+
+def fp64_report(rho, prs, acc, rho64, prs64, acc64):
+    """Relative errors of FP32 fields against FP64 ones: per particle for
+    density and pressure; per particle as |a - a64| / |a64| (median, max) and
+    against the field's largest magnitude for the acceleration, whose sums
+    cancel."""
+    def rel(x, y):
+        e = np.abs(x.astype(np.float64) - y)
+        return e / np.maximum(np.abs(y), 1e-30)
+
+    da = np.linalg.norm(acc.astype(np.float64) - acc64, axis=1)
+    na = np.linalg.norm(acc64, axis=1)
+    r_rho, r_p = rel(rho, rho64), rel(prs, prs64)
+    return {
+        "density": {"max_rel": float(r_rho.max()), "mean_rel": float(r_rho.mean())},
+        "pressure": {"max_rel": float(r_p.max()), "mean_rel": float(r_p.mean())},
+        "acceleration": {"max_abs_over_max": float(da.max() / na.max()),
+                         "median_rel": float(np.median(da / np.maximum(na, 1e-30))),
+                         "max_rel": float((da / np.maximum(na, 1e-30)).max())},
+    }
+
+
+def test_dam_break_1m_fields_against_fp64_oracle(gpu_lib, oracle, dam_break):
+    sc = dam_break
+    ref = oracle.step(sc.params, sc.terms, sc.particles, sc.mesh)
+    rho64, prs64, acc64 = oracle.fields_f64(ref.params, ref.sorted, ref.table)
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.upload(sc.particles)
+        g.step_until(STAGE_FORCES)
+        rho, prs, acc = g.fields()
+        _, perm = g.keys()
+    assert np.array_equal(perm, ref.perm)  # the FP64 fields are of the same sorted state
+    rep = fp64_report(rho, prs, acc, rho64, prs64, acc64)
+    print("FP32 GPU fields vs FP64 oracle, 1,048,576-particle dam break:", rep)
+    assert rep["density"]["max_rel"] <= 1e-5
+    assert rep["pressure"]["max_rel"] <= 1e-4
+    assert rep["acceleration"]["max_abs_over_max"] <= 1e-5
+    assert rep["acceleration"]["median_rel"] <= 1e-4
 
 
 def _run(sc, mode, substeps):

@@ -1,8 +1,12 @@
 """GPU substep against the golden fixtures: the outputs of the reference's own
 kernel sources (compiled as C++ by oracle/_ref and stored under tests/golden/),
 for the reference's initial lattice in scenes/cube.obj, a floor contact in
-scenes/box.obj, mucus in a corner, coincident particles, a 5-substep drop, and
-paths that cross mesh edges and corners exactly (ties between faces).
+scenes/box.obj, mucus in a corner, coincident particles, a 5-substep drop,
+paths that cross mesh edges and corners exactly (ties between faces), and
+paths aimed through the faces, edges and vertices of the reference's dense
+scenes monkey.obj (968 faces), shower.obj (1,248), labyrinth.obj (606) and
+river.obj (332), where the GPU's per-cell face lists must find the same hit
+as the reference's scan over every face.
 
 Bar: cell keys, sorted order, cell table and grid parameters bit-exact; the
 state after the substep within 1e-5 relative to each field's largest
@@ -21,6 +25,15 @@ pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = sorted(GOLDEN.glob("*.npz"))
 RTOL = 1e-5
+
+
+def golden_table(d):
+    """The fixture's dense cell table (compact fixtures: from the sorted keys)."""
+    if "table" in d:
+        return d["table"]
+    cells = int(d["params_out"][0]["grid_cell_count"])
+    return np.searchsorted(d["sorted"]["grid_index"], np.arange(cells, dtype=np.uint64),
+                           side="left").astype(np.uint32)
 
 
 def rel_err(a, b):
@@ -56,7 +69,7 @@ def test_substep_matches_reference_outputs(gpu_lib, path):
     if steps == 1:
         assert np.array_equal(keys, d["sorted"]["grid_index"])
         assert np.array_equal(perm, d["perm"])
-        assert np.array_equal(table, d["table"])
+        assert np.array_equal(table, golden_table(d))
         want_p = d["params_out"][0]
         for f in ("grid_size_x", "grid_size_y", "grid_size_z", "grid_cell_count"):
             assert prm[f] == want_p[f], f
