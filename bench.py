@@ -23,8 +23,12 @@ triangles), synthetic and seeded.
             OpenMP over particles, all host threads) on a bounded sample.
 
 --impl reference times the reference's CPU implementation of the path (the
-oracle port; the OpenCL CPU device is unavailable on these hosts) on a
-65,536-particle sample of the same workload per step, all host threads.
+oracle port; the OpenCL CPU device is unavailable on these hosts) on the same
+workload at full size, all host threads, the same --steps and --warmup, and
+prints the same `config`. Only a workload whose full-size substeps would take
+longer than REFERENCE_BUDGET_S in all (the pour's brute-force collision over
+131,072 triangles) is timed on a 65,536-particle sample, and its config then
+says so.
 
 Multi-GPU: a single scene does not shard (no halo exchange is built), so N
 ranks run N independent replicas of it (weak scaling); the batched workload
@@ -297,51 +301,88 @@ def cpu_baseline(scene, target_s: float = 12.0) -> dict:
                       f"({dt:.1f} s, OpenMP over particles)"}
 
 
+REFERENCE_BUDGET_S = 300.0  # longest full-size reference run (warm-up + timed substeps)
+
+
+def workload_config(scene, args, n_particles: int | None = None) -> dict:
+    """The `config` object of both arms' JSON lines (identical for the same
+    workload and flags)."""
+    return {
+        "workload": scene.name,
+        "n_particles": scene.n if n_particles is None else n_particles,
+        "lattice": scene.info.get("lattice"),
+        "box_m": scene.info.get("box"),
+        "h_m": scene.info.get("h"),
+        "scenes": scene.info.get("scenes", 1),
+        "faces": len(scene.mesh["indices"]) // 3,
+        "l2": ("inputs larger than L2: a substep moves about 600 B per particle through DRAM "
+               "(neighbour lists, records, state; profiles/dram_bytes_per_particle.json); the GPU "
+               "arm also writes a 256 MiB buffer before every timed launch, outside its events")
+              if not args.no_flush else
+              "inputs larger than L2: a substep moves about 600 B per particle through DRAM; no flush",
+    }
+
+
 def run_reference(args, world, rank) -> None:
     if rank != 0:
         return
     from oracle import Oracle
 
     scene = load_workload(args.workload)
-    if isinstance(scene, Batch):  # the first scenes, up to ~65k particles
-        take, tot = [], 0
-        for sc in scene.scenes:
-            if tot >= 65536:
-                break
-            take.append(sc)
-            tot += sc.n
-        sample_n = tot
-        sample = None
-    else:
-        sample_n = min(65536, scene.n)
-        sample = cpu_sample_scene(scene, sample_n)
     o = Oracle()
     threads = os.cpu_count() or 1
-    units = [sample] if sample is not None else take
+
+    def make_units(full: bool):
+        if full:
+            return scene.scenes if isinstance(scene, Batch) else [scene]
+        if isinstance(scene, Batch):  # the first scenes, up to ~65k particles
+            take, tot = [], 0
+            for sc in scene.scenes:
+                if tot >= 65536:
+                    break
+                take.append(sc)
+                tot += sc.n
+            return take
+        return [cpu_sample_scene(scene, min(65536, scene.n))]
+
+    units = make_units(True)
     cur = [u.particles for u in units]
 
     def one_step():
         for k, u in enumerate(units):
             cur[k] = o.run(u.params, u.terms, cur[k], 1, u.mesh, threads=threads)
 
-    for _ in range(args.warmup):
+    # the first warm-up substep at full size decides whether the whole run fits
+    t0 = time.perf_counter()
+    one_step()
+    first_s = time.perf_counter() - t0
+    full = first_s * (args.steps + args.warmup - 1) <= REFERENCE_BUDGET_S
+    if not full:
+        units = make_units(False)
+        cur = [u.particles for u in units]
         one_step()
+    for _ in range(args.warmup - 1):
+        one_step()
+    n_done = sum(u.n for u in units)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         one_step()
     dt = time.perf_counter() - t0
-    value = sample_n * args.steps / dt
+    value = n_done * args.steps / dt
+    what = (f"all {scene.n} particles per substep (the full workload)" if full else
+            f"{n_done} of the {scene.n} particles per substep (same spacing, mass, h, mesh): the full "
+            f"substep takes {first_s:.0f} s here")
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value,
         "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "strong" if isinstance(scene, Batch) else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene.name, "n_particles": sample_n, "full_n_particles": scene.n},
+        "config": workload_config(scene, args, None if full else n_done),
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample_n} of the {scene.n} particles (same spacing, mass, "
-                                   f"h, mesh) per substep; the reference's OpenCL CPU device has "
-                                   f"no platform on these hosts, so the oracle restatement of its "
-                                   f"kernels runs instead"},
+                         "sample": f"{what}; {args.steps} timed substeps after {args.warmup} warm-up "
+                                   f"substeps, OpenMP over particles on every host thread; the "
+                                   f"reference's OpenCL CPU device has no platform on these hosts, so "
+                                   f"the oracle restatement of its kernels runs instead"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -548,22 +589,10 @@ def main() -> None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": scene.name,
-            "n_particles": n,
-            "lattice": scene.info.get("lattice"),
-            "box_m": scene.info.get("box"),
-            "h_m": scene.info.get("h"),
-            "scenes": scene.info.get("scenes", 1),
-            "faces": len(scene.mesh["indices"]) // 3,
-            "l2": ("inputs larger than L2: a substep moves about 600 B per particle through DRAM "
-                   "(neighbour lists, records, state; profiles/dram_bytes_per_particle.json); in addition "
-                   f"a 256 MiB buffer is written before every timed launch of {unit} substep(s), outside "
-                   "the events") if not args.no_flush else
-                  "inputs larger than L2: a substep moves about 600 B per particle through DRAM; no flush",
-            "sim_s_per_s": value / n * float(scene.params["time_delta"] * scene.params["simulation_scale"]),
-            "wall_s_timed_region": wall,
-        },
+        "config": workload_config(scene, args),
+        "timed_launch_substeps": unit,
+        "sim_s_per_s": value / n * float(scene.params["time_delta"] * scene.params["simulation_scale"]),
+        "wall_s_timed_region": wall,
         "roofline": {
             "bound": "hbm",
             "kernel": dom,

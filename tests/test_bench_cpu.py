@@ -29,6 +29,16 @@ def test_reference_arm_line():
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert d["steps"] == 1 and d["warmup"] >= 3  # at least 3 warm-up steps, whatever is asked
     assert d["config"]["workload"] == "dam_break_32768"
+    # the full workload, with the GPU arm's config object
+    assert d["config"]["n_particles"] == 32768
+    sys.path.insert(0, str(ROOT))
+    import argparse
+
+    import bench
+    from libclsph_gb300 import workloads as W
+
+    assert d["config"] == bench.workload_config(W.dam_break_32k(), argparse.Namespace(no_flush=False))
+    assert "full workload" in d["cpu_baseline"]["sample"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
