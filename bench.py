@@ -389,6 +389,65 @@ def run_reference(args, world, rank) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_mlp_rows(args) -> None:
+    """`--workload mlp_1m_rows`: the learned stepper's fused MLP inference
+    kernels alone on 1,048,576 random standardised feature rows (random
+    weights): CUDA events around each launch after the warm-up launches, the
+    tcgen05 kernel (clsph_mlp_forward) and the mma.sync cross-check
+    (clsph_mlp_forward_mma_sync). FLOPs count 2 per multiply-add of the three
+    layers, 2 * rows * (32*256 + 256*256 + 256*4); the roofline is the
+    measured BF16 tensor peak."""
+    import torch
+
+    from libclsph_gb300 import learned as Lm
+
+    rows = 1 << 20
+    torch.cuda.set_device(0)
+    blob = np.zeros(Lm.BLOB, np.float32)
+    rng = np.random.default_rng(0)
+    blob[:Lm.N_PARAMS] = rng.normal(0, 0.05, Lm.N_PARAMS)
+    blob[Lm.OFF_XSIGMA:Lm.OFF_YMU] = 1
+    blob[Lm.OFF_YSIGMA:] = 1
+    net = Lm.Mlp(blob=blob)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(rows, Lm.N_FEATURES, device="cuda", generator=g).to(torch.bfloat16)
+    y = torch.empty(rows, Lm.N_OUTPUTS, device="cuda")
+    flops = 2.0 * rows * (32 * 256 + 256 * 256 + 256 * 4)
+    peaks = ROOT / "MEASURED_PEAKS.json"
+    peak = json.loads(peaks.read_text()).get("bf16_tflops") if peaks.exists() else None
+    peak_kind = "measured" if peak else "fallback"
+    peak = peak or 1900.0
+    out = {}
+    for name, fn in (("tcgen05", net.forward), ("mma_sync", net.forward_mma_sync)):
+        for _ in range(args.warmup):
+            fn(x.data_ptr(), rows, y.data_ptr())
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        for a, b in ev:
+            a.record()
+            fn(x.data_ptr(), rows, y.data_ptr())
+            b.record()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+        out[name] = {"ms": ms, "tflops": flops / ms / 1e9}
+    status = net.status()
+    net.close()
+    tc = out["tcgen05"]
+    line = {
+        "metric": "TFLOP/s", "value": tc["tflops"], "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tc["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulation)", "data": "synthetic",
+        "config": {"workload": "mlp_1m_rows", "rows": rows, "layers": "32-256-256-4, GELU",
+                   "l2": "64 MB of feature rows per launch, no flush"},
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_tc", "achieved": tc["tflops"], "peak": peak,
+                     "peak_kind": peak_kind, "unit": "TFLOP/s", "frac": tc["tflops"] / peak,
+                     "traffic": None},
+        "mma_sync": out["mma_sync"], "device_status": status, "gpu_launches": 2 * (args.steps + args.warmup),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def learned_evaluation(scene, solver) -> dict | None:
     """Plain vs learned 4x-dt over the time of 2000 plain substeps, with the 1 %
     density check and without it (weights from
@@ -431,7 +490,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dam_break_1m", choices=sorted(WORKLOADS) + ["mlp_1m_rows"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
@@ -445,6 +504,9 @@ def main() -> None:
     if args.impl == "reference":
         run_reference(args, world, rank)
         barrier(world)
+        return
+    if args.workload == "mlp_1m_rows":
+        run_mlp_rows(args)
         return
 
     import torch

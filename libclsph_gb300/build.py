@@ -101,8 +101,10 @@ def build_host(force: bool = False) -> Path | None:
     return HOST_SO
 
 
-def build_all(force: bool = False, with_oracle: bool = True) -> None:
-    """Compiles every native part; the GPU engine first (the host layer links it)."""
+def build_all(force: bool = False, with_oracle: bool = False) -> None:
+    """Compiles every native part of the library; the GPU engine first (the
+    host layer links it). with_oracle also builds the CPU checkers under
+    oracle/ (test infrastructure, never part of the library)."""
     jobs = []
     with ThreadPoolExecutor(max_workers=3) as ex:
         gpu = ex.submit(build_gpu, force)
@@ -116,12 +118,13 @@ def build_all(force: bool = False, with_oracle: bool = True) -> None:
 
 
 def _build_oracles() -> None:
+    """oracle/liboracle.so, and oracle/_ref where the reference sources are
+    present (the Makefile decides; CLSPH_REFERENCE_ROOT points elsewhere)."""
     oracle_dir = ROOT / "oracle"
     if not (oracle_dir / "Makefile").exists():
         return
     _run(["make", "-s", "-C", str(oracle_dir), "liboracle.so"])
-    if Path("/root/reference/libclsph/kernels").is_dir():
-        _run(["make", "-s", "-C", str(oracle_dir), "ref"])
+    _run(["make", "-s", "-C", str(oracle_dir), "ref-if-present"])
 
 
 if __name__ == "__main__":

@@ -33,11 +33,28 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_SO
 
 
-def build_ref(reference_root: str = "/root/reference") -> Path | None:
+def _make_args(reference_root: str | None) -> list[str]:
+    """REF=... for the Makefile: the argument, else CLSPH_REFERENCE_ROOT, else
+    the Makefile's own default."""
+    root = reference_root or os.environ.get("CLSPH_REFERENCE_ROOT")
+    return [f"REF={root}"] if root else []
+
+
+def reference_root() -> Path:
+    """Where the reference checkout is looked for (CLSPH_REFERENCE_ROOT, else
+    the Makefile's default); it may not exist on this machine."""
+    out = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref", *_make_args(None)],
+                         capture_output=True, text=True)
+    return Path(out.stdout.strip() or "/nonexistent")
+
+
+def build_ref(reference_root: str | None = None) -> Path | None:
     """Builds oracle/_ref when the reference sources are present; else None."""
-    if not Path(reference_root, "libclsph", "kernels").is_dir():
+    args = _make_args(reference_root)
+    if subprocess.run(["make", "-s", "-C", str(HERE), "has-ref", *args],
+                      capture_output=True).returncode != 0:
         return None
-    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={reference_root}"], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", *args], check=True)
     return REF_SO
 
 
@@ -222,10 +239,13 @@ class RefBuild(_StepLib):
 
 
 def have_ref() -> bool:
-    return REF_SO.exists() or Path("/root/reference/libclsph/kernels").is_dir()
+    if REF_SO.exists():
+        return True
+    return subprocess.run(["make", "-s", "-C", str(HERE), "has-ref", *_make_args(None)],
+                          capture_output=True).returncode == 0
 
 
-__all__ = ["Oracle", "RefBuild", "StepResult", "build_oracle", "build_ref", "have_ref",
+__all__ = ["Oracle", "RefBuild", "StepResult", "build_oracle", "build_ref", "have_ref", "reference_root",
            "ORACLE_SO", "REF_SO"]
 
 os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")

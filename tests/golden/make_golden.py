@@ -29,7 +29,9 @@ from libclsph_gb300.layout import particles_from_arrays  # noqa: E402
 from libclsph_gb300.settings import WATER, DEFAULT_SIM, settings_from_dicts  # noqa: E402
 from oracle import RefBuild, build_ref  # noqa: E402
 
-REF_ROOT = Path("/root/reference")
+from oracle import reference_root  # noqa: E402
+
+REF_ROOT = reference_root()  # CLSPH_REFERENCE_ROOT, else oracle/Makefile's default
 MUCUS = {"fluid_density": 1000, "dynamic_viscosity": 36, "restitution": 0.5, "k": 5,
          "surface_tension_threshold": 5, "surface_tension": 6,
          "particles_inside_influence_radius": 40}

@@ -100,7 +100,9 @@ def test_project_example_compiles(tmp_path):
 
 
 def test_reference_example_compiles_unchanged(tmp_path):
-    src = Path("/root/reference/example/particles.cpp")
+    from oracle import reference_root
+
+    src = reference_root() / "example" / "particles.cpp"
     if not src.exists():
         pytest.skip("reference sources not present")
     r = compile_against_dropin(src, tmp_path / "particles")

@@ -17,7 +17,14 @@ from libclsph_gb300.simulation import HoudiniFileSaver, init_lattice
 
 ROOT = Path(__file__).resolve().parents[1]
 HOST_SO = ROOT / "libclsph_gb300" / "_lib" / "libclsph.so"
-REF_SCENES = Path("/root/reference/scenes")
+def _reference_root():
+    from oracle import reference_root
+
+    return reference_root()
+
+
+REF_ROOT = _reference_root()  # the reference checkout, where this machine has one
+REF_SCENES = REF_ROOT / "scenes"
 
 
 @pytest.fixture(scope="module")
@@ -98,7 +105,7 @@ def test_water_default_h():
 
 
 def test_reference_property_files(host):
-    base = Path("/root/reference")
+    base = REF_ROOT
     if not base.is_dir():
         pytest.skip("reference files not present")
     for fluid in ("water", "mucus"):
