@@ -249,12 +249,63 @@ def collided(st, r) -> int:
     return int(np.sum(np.linalg.norm(r.final["position"][:, :3] - free, axis=1) > 1e-5))
 
 
+GEO_NAME = "frame_ref_300"
+
+
+def make_geo_golden() -> None:
+    """The reference's own .geo frame writer (oracle/_ref/ref_geo: the
+    reference's houdini_file_saver.cpp and HoudiniFileDumpHelper.cpp compiled
+    unchanged) on 300 particles whose densities cover every branch of its
+    colour ramp (below 0, the 500 / 1000 / 1500 / 2000 boundaries, above
+    2000) and whose coordinates span many magnitudes and signs (the stream's
+    default 6-significant-digit formatting, exponents, -0). Writes
+    tests/golden/frame_ref_300.npz (inputs) and frame_ref_300.geo (output)."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    from libclsph_gb300.layout import PARAMS, PARTICLE
+
+    rng = np.random.default_rng(20)
+    n = 300
+    parts = np.zeros(n, dtype=PARTICLE)
+    scale = 10.0 ** rng.integers(-7, 4, (n, 1))
+    parts["position"][:, :3] = (rng.normal(0, 1, (n, 3)) * scale).astype(np.float32)
+    parts["velocity"][:, :3] = (rng.normal(0, 1, (n, 3)) * scale[::-1]).astype(np.float32)
+    parts["intermediate_velocity"][:, :3] = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    parts["position"][0, :3] = [-0.0, 0.0, 1.0]
+    parts["velocity"][1, :3] = [123456.789, -0.000123456789, 1e-30]
+    dens = rng.uniform(-100, 2600, n).astype(np.float32)
+    edges = [-1.0, 0.0, 1e-3, 250.0, 499.99997, 500.0, 500.00003, 750.0, 999.99994, 1000.0,
+             1000.0001, 1250.0, 1499.9999, 1500.0, 1500.0001, 1800.0, 1999.9999, 2000.0,
+             2000.0002, 3000.0]
+    dens[2:2 + len(edges)] = np.array(edges, dtype=np.float32)
+    parts["density"] = dens
+    parts["pressure"] = rng.normal(0, 1e4, n).astype(np.float32)
+    parts["grid_index"] = rng.integers(0, 1 << 20, n).astype(np.uint32)
+    params = np.zeros(1, dtype=PARAMS)
+    params["particles_count"] = n
+    params["particle_mass"] = np.float32(7.9717e-4)
+    with tempfile.TemporaryDirectory() as tmp:
+        t = Path(tmp)
+        (t / "frames").mkdir()
+        params.tofile(t / "params.bin")
+        parts.tofile(t / "particles.bin")
+        subprocess.run([str(ROOT / "oracle" / "_ref" / "ref_geo"), str(t / "params.bin"),
+                        str(t / "particles.bin"), str(t) + "/"], check=True)
+        shutil.copyfile(t / "frames" / "frame0000001.geo", HERE / f"{GEO_NAME}.geo")
+    np.savez_compressed(HERE / f"{GEO_NAME}.npz", params=params, particles=parts)
+    print(GEO_NAME, (HERE / f"{GEO_NAME}.geo").stat().st_size, "bytes")
+
+
 def main() -> None:
     """Writes every fixture, or only those named on the command line (the
     others keep their files and manifest entries)."""
     if build_ref() is None:
         raise SystemExit("reference sources not found; fixtures are generated in the dev container")
     only = set(sys.argv[1:])
+    if not only or GEO_NAME in only:
+        make_geo_golden()
     ref = RefBuild()
     mpath = HERE / "manifest.json"
     manifest = json.loads(mpath.read_text()) if only and mpath.exists() else {}

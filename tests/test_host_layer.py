@@ -274,6 +274,24 @@ def test_houdini_writer_python_and_cpp_agree(tmp_path, host):
     assert a.rstrip().endswith("beginExtra\nendExtra")
 
 
+def test_houdini_writers_match_reference_frame(tmp_path, host):
+    """Both writers against tests/golden/frame_ref_300.geo, written by the
+    reference's own houdini_file_saver.cpp + HoudiniFileDumpHelper.cpp
+    (oracle/_ref/ref_geo, tests/golden/make_golden.py): every density branch
+    of the colour ramp, coordinates from 1e-7 to 1e3, -0 and exponents."""
+    golden = Path(__file__).resolve().parent / "golden"
+    d = np.load(golden / "frame_ref_300.npz")
+    parts, params = d["particles"], d["params"]
+    want = (golden / "frame_ref_300.geo").read_bytes()
+    (tmp_path / "py" / "frames").mkdir(parents=True)
+    (tmp_path / "cpp" / "frames").mkdir(parents=True)
+    HoudiniFileSaver(str(tmp_path / "py") + "/").writeFrameToFile(parts, params[0])
+    assert host.clsph_host_write_houdini((str(tmp_path / "cpp") + "/").encode(), parts.ctypes.data,
+                                         params.ctypes.data) == 0
+    assert (tmp_path / "py" / "frames" / "frame0000001.geo").read_bytes() == want
+    assert (tmp_path / "cpp" / "frames" / "frame0000001.geo").read_bytes() == want
+
+
 def test_houdini_writer_parallel_formatting_is_byte_identical(tmp_path, host):
     """A frame large enough for the C++ writer's threaded formatting."""
     rng = np.random.default_rng(4)
