@@ -259,7 +259,8 @@ def make_geo_golden() -> None:
     colour ramp (below 0, the 500 / 1000 / 1500 / 2000 boundaries, above
     2000) and whose coordinates span many magnitudes and signs (the stream's
     default 6-significant-digit formatting, exponents, -0). Writes
-    tests/golden/frame_ref_300.npz (inputs) and frame_ref_300.geo (output)."""
+    tests/golden/geo/frame_ref_300.npz (inputs) and frame_ref_300.geo (output),
+    outside the substep fixtures' folder."""
     import shutil
     import subprocess
     import tempfile
@@ -293,9 +294,10 @@ def make_geo_golden() -> None:
         parts.tofile(t / "particles.bin")
         subprocess.run([str(ROOT / "oracle" / "_ref" / "ref_geo"), str(t / "params.bin"),
                         str(t / "particles.bin"), str(t) + "/"], check=True)
-        shutil.copyfile(t / "frames" / "frame0000001.geo", HERE / f"{GEO_NAME}.geo")
-    np.savez_compressed(HERE / f"{GEO_NAME}.npz", params=params, particles=parts)
-    print(GEO_NAME, (HERE / f"{GEO_NAME}.geo").stat().st_size, "bytes")
+        (HERE / "geo").mkdir(exist_ok=True)
+        shutil.copyfile(t / "frames" / "frame0000001.geo", HERE / "geo" / f"{GEO_NAME}.geo")
+    np.savez_compressed(HERE / "geo" / f"{GEO_NAME}.npz", params=params, particles=parts)
+    print(GEO_NAME, (HERE / "geo" / f"{GEO_NAME}.geo").stat().st_size, "bytes")
 
 
 def main() -> None:

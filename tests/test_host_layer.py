@@ -275,11 +275,11 @@ def test_houdini_writer_python_and_cpp_agree(tmp_path, host):
 
 
 def test_houdini_writers_match_reference_frame(tmp_path, host):
-    """Both writers against tests/golden/frame_ref_300.geo, written by the
+    """Both writers against tests/golden/geo/frame_ref_300.geo, written by the
     reference's own houdini_file_saver.cpp + HoudiniFileDumpHelper.cpp
     (oracle/_ref/ref_geo, tests/golden/make_golden.py): every density branch
     of the colour ramp, coordinates from 1e-7 to 1e3, -0 and exponents."""
-    golden = Path(__file__).resolve().parent / "golden"
+    golden = Path(__file__).resolve().parent / "golden" / "geo"
     d = np.load(golden / "frame_ref_300.npz")
     parts, params = d["particles"], d["params"]
     want = (golden / "frame_ref_300.geo").read_bytes()

@@ -77,7 +77,11 @@ def test_oracle_under_sanitizers(cxx, tmp_path):
     from oracle import Oracle
 
     want = Oracle().run(sc.params, sc.terms, sc.particles, steps, mesh=sc.mesh, threads=2)
-    assert got == want.tobytes()
+    # every field of the 80-byte records; bytes 76-79 are the struct's tail
+    # padding, which neither program defines
+    a = np.frombuffer(got, np.uint8).reshape(-1, 80)[:, :76]
+    b = want.view(np.uint8).reshape(-1, 80)[:, :76]
+    assert np.array_equal(a, b)
 
 
 def test_host_layer_under_sanitizers(cxx, tmp_path):
