@@ -208,13 +208,49 @@ int clsph_gpu_set_launch_shape(clsph_gpu* h, int density_block, int forces_block
  *    half in shared memory once for all of the cell's particles. The default;
  *  PARTICLE_WARPS: one warp per particle tests 32 candidates at a time (for
  *    scenes too small to fill the GPU otherwise).
- * The block size of clsph_gpu_set_launch_shape applies to WINDOW only. */
+ * The density block size of clsph_gpu_set_launch_shape sets WINDOW's block
+ * (64 or 128 threads; 256 runs as 128) and CELL_WARPS' staging tiles per
+ * block (64 / 128 / 256 threads = 2 / 4 / 8 warps, each staging 32
+ * candidates at a time); clsph_gpu_autotune tries every combination. */
 enum {
   CLSPH_SEARCH_WINDOW = 0,
   CLSPH_SEARCH_CELL_WARPS = 1,
   CLSPH_SEARCH_PARTICLE_WARPS = 2
 };
 int clsph_gpu_set_neighbour_search(clsph_gpu* h, int mode);
+
+/* Runs whole substeps as one persistent launch (no counterpart in the
+ * reference): every phase of the substep in one cooperative kernel of 256-
+ * thread blocks, all resident at once, separated by grid-wide barriers,
+ * up to 64 substeps per launch, for handles of any number of scenes. The
+ * results equal the launched substeps' bit for bit (the same block-level
+ * code); clsph_gpu_autotune keeps whichever form is faster. Neighbour search
+ * is CELL_WARPS with 8 warps per block; per-kernel profiling and
+ * clsph_gpu_step_until launch the kernels as usual. CLSPH_ERR_CUDA if the
+ * device has no cooperative launch. */
+int clsph_gpu_set_persistent(clsph_gpu* h, int enabled);
+
+/* Bound of each grid-barrier wait of the persistent launch (default
+ * CLSPH_DEFAULT_BARRIER_SPINS, about seconds) and a test hook of its failure
+ * path: block `withheld_block` (CLSPH_NO_BLOCK in normal use) leaves at the
+ * first barrier, as a block that never arrives, so every other block's wait
+ * runs out; clsph_gpu_sync then returns CLSPH_ERR_CUDA and resets the
+ * barrier. */
+#define CLSPH_DEFAULT_BARRIER_SPINS (1u << 22)
+#define CLSPH_NO_BLOCK 0xFFFFFFFFu
+int clsph_gpu_set_barrier_limits(clsph_gpu* h, uint32_t barrier_spins, uint32_t withheld_block);
+
+/* The per-cell triangle lists of a scene's mesh, as built on the device by
+ * clsph_gpu_set_scene_mesh (an inspection call: the collision loop of
+ * libclsph/kernels/collisions.cl:91-129 scans every face; the engine scans
+ * the list of the cell a segment starts in, which holds, in ascending order,
+ * every face whose box grown by the list reach and a tolerance meets the
+ * cell). sizes[0] = cells + 1 (CSR starts), sizes[1] = list entries (both 0
+ * without lists: an empty or non-finite mesh); plan (10 floats, may be NULL)
+ * = grid origin xyz, cell edge, pad, tolerance, dims xyz, reach. A NULL
+ * cell_start or cell_faces skips that copy. */
+int clsph_gpu_read_face_lists(clsph_gpu* h, uint32_t scene, float* plan, uint32_t* cell_start,
+                              uint64_t start_cap, uint32_t* cell_faces, uint64_t faces_cap, uint32_t* sizes);
 
 /* Bounds of the engine's device-side waits; no counterpart in the reference,
  * whose OpenCL queue has no device-side waits. radix_lookback_spins bounds

@@ -17,6 +17,7 @@
 
 #include "clsph_gpu.h"
 #include "clsph_handle.cuh"
+#include "clsph_mesh.cuh"
 
 static_assert(sizeof(clsph_particle) == 80, "particle layout");
 static_assert(sizeof(clsph_parameters) == 128, "parameter layout");
@@ -26,6 +27,8 @@ static_assert(offsetof(clsph_parameters, min_point) == 96, "parameter layout");
 static_assert(sizeof(clsph_kernel_terms) == 20, "kernel constant layout");
 static_assert(kRadixLookbackSpins == CLSPH_DEFAULT_LOOKBACK_SPINS, "default look-back bound");
 static_assert(kNoTile == CLSPH_NO_TILE, "withheld-tile sentinel");
+static_assert(kBarrierSpins == CLSPH_DEFAULT_BARRIER_SPINS, "default barrier bound");
+static_assert(kNoBlock == CLSPH_NO_BLOCK, "withheld-block sentinel");
 
 namespace clsph_host {
 
@@ -71,7 +74,10 @@ Consts derive_consts(const clsph_parameters& p, const clsph_kernel_terms& t, uin
   c.visc = t.viscosity;
   // smoothing.cl:24: -45 / (float)(M_PI * pown(h, 6)) with M_PI in double
   c.spiky_zero = -45.f / (float)(M_PI * (double)pown_f(p.h, 6));
-  c.cull_r2 = p.h * p.h * 1.0001f;
+  // conservative h^2 of the FMA culls: 5e-4 above h^2, five times the largest
+  // rounding of the cell-relative cull (k_density_cells) and far above that
+  // of the direct differences; the exact test decides
+  c.cull_r2 = p.h * p.h * 1.0005f;
   return c;
 }
 
@@ -103,33 +109,37 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   h->ids_sel = dst_ids;
   if (until <= CLSPH_STAGE_SORT) return 0;
   {
-    const int b = h->density_block;
+    // the window mode's per-thread tables fit shared memory up to 128 threads
+    const int b = h->density_block == 64 ? 64 : 128;
     const dim3 grid((n + b - 1) / b);
     auto args = [&](auto kernel) {
       h->launch(K_DENSITY, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys,
                 (const float4*)h->st[1].pos, h->ci, (const Consts*)h->consts, h->aux, h->nlist,
-                h->ncount, h->nlist_cap, (const float4*)h->st[1].vel, h->frec);
+                h->ncount, h->nlist_cap, (const float4*)h->st[1].vel, h->frec, h->nb_start);
     };
-    auto cells = [&](auto kernel) {
-      h->launch(K_DENSITY, kernel, dim3(h->sm_count * 16), dim3(kCellWarps * 32),
+    // cell-warp mode: the block size sets the warps (cell staging tiles) per
+    // block, 2, 4 or 8, each with its own 32-candidate tile and buffers
+    auto cells = [&](auto kernel, int warps) {
+      h->launch(K_DENSITY, kernel, dim3(h->sm_count * (64 / warps)), dim3(warps * 32),
                 n, (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, cctl,
                 (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci,
                 (const Consts*)h->consts, h->aux, h->nlist, h->ncount, h->nlist_cap,
                 (const float4*)h->st[1].vel, h->frec, (const uint32_t*)h->cell_list,
-                h->step_counters);
+                h->step_counters, h->nb_start);
     };
     if (h->search == CLSPH_SEARCH_CELL_WARPS) {
-      cells(k_density_cells<kCellWarps>);
+      if (h->density_block == 64) cells(k_density_cells<2>, 2);
+      else if (h->density_block == 256) cells(k_density_cells<8>, 8);
+      else cells(k_density_cells<kCellWarps>, kCellWarps);
     } else if (h->search == CLSPH_SEARCH_PARTICLE_WARPS) {
       h->launch(K_DENSITY, k_density_pwarp, dim3((n + kParticleWarps - 1) / kParticleWarps),
                 dim3(kParticleWarps * 32), n, (const DevGrid*)h->grids, (const uint16_t*)h->scene_of,
                 cctl, (const uint32_t*)h->keys, (const float4*)h->st[1].pos, h->ci,
                 (const Consts*)h->consts, h->aux, h->nlist, h->ncount, h->nlist_cap,
-                (const float4*)h->st[1].vel, h->frec);
+                (const float4*)h->st[1].vel, h->frec, h->nb_start);
     } else {
       if (b == 64) args(k_density<64>);
-      else if (b == 256) args(k_density<256>);
       else args(k_density<128>);
     }
   }
@@ -140,8 +150,9 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
     auto args = [&](auto kernel) {
       h->launch(K_FORCES, kernel, grid, dim3(b), n, (const DevGrid*)h->grids,
                 (const uint16_t*)h->scene_of, cctl, (const uint32_t*)h->keys, h->st[1],
-                (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-                (const uint32_t*)h->ncount, h->nlist_cap, h->acc, NoForceHook{}, (const float4*)h->frec);
+                (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint16_t*)h->nlist,
+                (const uint32_t*)h->ncount, h->nlist_cap, h->acc, NoForceHook{}, (const float4*)h->frec,
+                (const uint32_t*)h->nb_start);
     };
     if (b == 64) args(k_forces<64>);
     else if (b == 256) args(k_forces<256>);
@@ -149,6 +160,68 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   }
   if (until <= CLSPH_STAGE_FORCES) return 0;
   return enqueue_advect(h);
+}
+
+// Runs `substeps` substeps as one persistent cooperative launch per at most
+// 64 substeps (clsph_persistent.cuh).
+int clsph_host::launch_persistent(clsph_gpu* h, uint32_t substeps) {
+  if (!h->persist_blocks) {
+    int per_sm = 0, coop = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+    if (!coop) return fail(CLSPH_ERR_CUDA, "persistent substeps: the device has no cooperative launch");
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substeps_persistent, kPersistThreads, 0));
+    if (per_sm < 1) return fail(CLSPH_ERR_CUDA, "persistent substeps: no resident block fits an SM");
+    h->persist_blocks = (uint32_t)per_sm * h->sm_count;
+  }
+  PersistArgs a{};
+  a.n = h->n;
+  a.nscenes = h->nscenes;
+  a.ntiles = h->ntiles;
+  a.slots = h->slots;
+  a.nlist_cap = h->nlist_cap;
+  a.max_iters = h->max_iters;
+  a.bbox = h->bbox;
+  a.grids = h->grids;
+  a.scene_h = h->scene_h;
+  a.status = h->status;
+  a.digit_total = h->digit_total;
+  a.step_counters = h->step_counters;
+  a.ctl = h->ctl;
+  a.scene_of = h->scene_of;
+  a.keys = h->keys;
+  a.vals = h->vals;
+  a.lookback = h->lookback;
+  a.st[0] = h->st[0];
+  a.st[1] = h->st[1];
+  a.ids[0] = h->ids[0];
+  a.ids[1] = h->ids[1];
+  a.ci = h->ci;
+  a.cell_list = h->cell_list;
+  a.consts = h->consts;
+  a.aux = h->aux;
+  a.nlist = h->nlist;
+  a.ncount = h->ncount;
+  a.frec = h->frec;
+  a.nb_start = h->nb_start;
+  a.acc = h->acc;
+  a.meshes = h->meshes;
+  a.capped = h->capped;
+  a.barrier = h->pbar;
+  a.spin_limit = h->radix_spin_limit;
+  a.withheld_tile = h->radix_withheld_tile;
+  a.barrier_limit = h->barrier_limit;
+  a.withheld_block = h->withheld_block;
+  for (uint32_t done = 0; done < substeps;) {
+    uint32_t count = std::min<uint32_t>(substeps - done, 64u);
+    uint32_t sel = (uint32_t)h->ids_sel;
+    void* args[] = {&a, &count, &sel};
+    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_substeps_persistent, dim3(h->persist_blocks),
+                                         dim3(kPersistThreads), args, 0, h->stream));
+    ++h->launches;
+    h->ids_sel ^= (int)(count & 1u);
+    done += count;
+  }
+  return 0;
 }
 
 int clsph_host::enqueue_advect(clsph_gpu* h) {
@@ -210,14 +283,13 @@ int read_grid(clsph_gpu* h, uint32_t scene, DevGrid* g, uint32_t* ctl) {
   return 0;
 }
 
-// Per-cell triangle lists over a uniform grid around the mesh. Every face
-// whose bounding box, grown by the list reach plus a tolerance, overlaps a
-// cell is listed there in ascending face order, so scanning one list equals
-// the reference's scan over all faces for any segment that starts in the
-// cell and is no longer than the reach.
-int build_face_grid(const clsph_parameters& p, const float* vx, uint32_t nv, const uint32_t* ix,
-                    uint32_t faces, std::vector<uint32_t>& start, std::vector<uint32_t>& list,
-                    DevMesh& mesh) {
+// Plan of the per-cell triangle lists (clsph_mesh.cuh): a uniform grid
+// around the mesh's bounding box, padded by the list reach (the longest
+// segment one list serves: 1.5 x the largest distance a particle moves in a
+// substep, plus 2 mm) and a rounding tolerance, with at most 2^22 cells.
+// Returns 1 for a non-finite mesh (then every face is scanned).
+int plan_face_grid(const clsph_parameters& p, const float* vx, uint32_t nv, const uint32_t* ix,
+                   uint32_t faces, FaceGridPlan& g, float& reach) {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (uint32_t f = 0; f < faces; ++f)
     for (int k = 0; k < 3; ++k) {
@@ -225,83 +297,82 @@ int build_face_grid(const clsph_parameters& p, const float* vx, uint32_t nv, con
       if (v >= nv) return fail(CLSPH_ERR_ARGUMENT, "mesh index out of range");
       for (int a = 0; a < 3; ++a) {
         float c = vx[3 * v + a];
-        if (!std::isfinite(c)) return 1;  // non-finite mesh: scan every face instead
+        if (!std::isfinite(c)) return 1;
         lo[a] = std::fmin(lo[a], c);
         hi[a] = std::fmax(hi[a], c);
       }
     }
   float extent = 0.f;
   for (int a = 0; a < 3; ++a) extent = std::fmax(extent, hi[a] - lo[a]);
-  const float reach = std::fmax(p.max_velocity * p.time_delta * p.simulation_scale * 1.5f + 0.002f, 1e-4f);
+  reach = std::fmax(p.max_velocity * p.time_delta * p.simulation_scale * 1.5f + 0.002f, 1e-4f);
   const float tol = 1e-4f * extent + 1e-5f;
   const float pad = reach + tol;
-  float glo[3], ghi[3];
+  float ghi[3];
   for (int a = 0; a < 3; ++a) {
-    glo[a] = lo[a] - pad;
+    g.glo[a] = lo[a] - pad;
     ghi[a] = hi[a] + pad;
   }
   float cell = std::fmax((extent + 2 * pad) / 128.f, pad);
-  int dims[3];
   for (;;) {
     double total = 1.0;
     for (int a = 0; a < 3; ++a) {
-      dims[a] = (int)std::ceil((ghi[a] - glo[a]) / cell);
-      if (dims[a] < 1) dims[a] = 1;
-      total *= dims[a];
+      g.dims[a] = (int)std::ceil((ghi[a] - g.glo[a]) / cell);
+      if (g.dims[a] < 1) g.dims[a] = 1;
+      total *= g.dims[a];
     }
     if (total <= (double)(1u << 22)) break;
     cell *= 1.25f;
   }
-  const size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
-  auto cell_range = [&](const float* mn, const float* mx, int* c0, int* c1) {
-    for (int a = 0; a < 3; ++a) {
-      int a0 = (int)std::floor((mn[a] - glo[a]) / cell);
-      int a1 = (int)std::floor((mx[a] - glo[a]) / cell);
-      c0[a] = a0 < 0 ? 0 : (a0 >= dims[a] ? dims[a] - 1 : a0);
-      c1[a] = a1 < 0 ? 0 : (a1 >= dims[a] ? dims[a] - 1 : a1);
-    }
-  };
-  std::vector<uint32_t> count(ncell + 1, 0u);
-  for (int pass = 0; pass < 2; ++pass) {
-    for (uint32_t f = 0; f < faces; ++f) {
-      float mn[3], mx[3];
-      for (int a = 0; a < 3; ++a) {
-        float c0 = vx[3 * ix[3 * f] + a], c1 = vx[3 * ix[3 * f + 1] + a], c2 = vx[3 * ix[3 * f + 2] + a];
-        mn[a] = std::fmin(c0, std::fmin(c1, c2)) - pad - tol;
-        mx[a] = std::fmax(c0, std::fmax(c1, c2)) + pad + tol;
-      }
-      int c0[3], c1[3];
-      cell_range(mn, mx, c0, c1);
-      for (int z = c0[2]; z <= c1[2]; ++z)
-        for (int y = c0[1]; y <= c1[1]; ++y)
-          for (int x = c0[0]; x <= c1[0]; ++x) {
-            size_t c = ((size_t)z * dims[1] + y) * dims[0] + x;
-            if (pass == 0)
-              count[c]++;
-            else
-              list[start[c] + count[c]++] = f;
-          }
-    }
-    if (pass == 0) {
-      start.assign(ncell + 1, 0u);
-      uint64_t run = 0;
-      for (size_t c = 0; c < ncell; ++c) {
-        start[c] = (uint32_t)run;
-        run += count[c];
-        if (run > 0xFFFFFFFFull) return fail(CLSPH_ERR_TOO_LARGE, "face lists too large");
-      }
-      start[ncell] = (uint32_t)run;
-      list.assign(run ? run : 1, 0u);
-      std::fill(count.begin(), count.end(), 0u);
-    }
-  }
-  for (int a = 0; a < 3; ++a) {
-    mesh.lo[a] = glo[a];
-    mesh.dims[a] = dims[a];
-  }
-  mesh.inv_cell = 1.f / cell;
-  mesh.reach = reach;
+  g.cell = cell;
+  g.pad = pad;
+  g.tol = tol;
+  g.cells = (uint32_t)g.dims[0] * (uint32_t)g.dims[1] * (uint32_t)g.dims[2];
   return 0;
+}
+
+// Builds the lists of an uploaded mesh on the device (clsph_mesh.cuh) into
+// sm.cell_start / sm.cell_faces.
+int build_face_lists(clsph_gpu* h, SceneMesh& sm, uint32_t faces, const FaceGridPlan& g) {
+  const uint32_t cells = g.cells;
+  const uint32_t fblocks = grid_blocks(faces, h->sm_count * 8);
+  uint32_t *count = nullptr, *sums = nullptr, *fill = nullptr;
+  unsigned long long* entries = nullptr;
+  int rc = 0;
+  auto done = [&](int code) {
+    cudaFree(count);
+    cudaFree(sums);
+    cudaFree(fill);
+    cudaFree(entries);
+    return code;
+  };
+  const uint32_t sblocks = (cells + kScanBlock - 1) / kScanBlock;
+  if ((rc = dev_alloc(&count, cells)) || (rc = dev_alloc(&sums, sblocks + 1)) || (rc = dev_alloc(&fill, cells)) ||
+      (rc = dev_alloc(&entries, 1)) || (rc = dev_alloc(&sm.cell_start, (size_t)cells + 1)))
+    return done(rc);
+  cudaStream_t s = h->stream;
+  cudaError_t e = cudaMemsetAsync(entries, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(uint32_t) * cells, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(fill, 0, sizeof(uint32_t) * cells, s);
+  if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
+  k_face_entries<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, entries);
+  unsigned long long total = 0;
+  e = cudaMemcpyAsync(&total, entries, sizeof(total), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
+  if (total > 0x7FFFFFFFull) return done(fail(CLSPH_ERR_TOO_LARGE, "face lists too large"));
+  if ((rc = dev_alloc(&sm.cell_faces, total ? total : 1))) return done(rc);
+  k_face_count<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, count);
+  k_scan_sums<<<sblocks, kScanThreads, 0, s>>>(count, cells, sums);
+  k_scan_top<<<1, kScanThreads, 0, s>>>(sums, sblocks, sm.cell_start + cells);
+  k_scan_apply<<<sblocks, kScanThreads, 0, s>>>(count, cells, sums, sm.cell_start);
+  k_face_fill<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, sm.cell_start, fill, sm.cell_faces);
+  k_face_sort<<<grid_blocks(cells, h->sm_count * 8), kBlock, 0, s>>>(sm.cell_start, cells, sm.cell_faces);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
+  sm.plan = g;
+  sm.list_len = (uint32_t)total;
+  return done(0);
 }
 
 int sync_scene_tables(clsph_gpu* h) {
@@ -373,6 +444,7 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
   while ((1u << log2s) < slots) ++log2s;
   if ((rc = dev_alloc(&h->aux, n)) || (rc = dev_alloc(&h->acc, n)) || (rc = dev_alloc(&h->frec, 2 * (size_t)n)) ||
       (rc = dev_alloc(&h->nlist, (size_t)h->nlist_cap * n)) || (rc = dev_alloc(&h->ncount, n)) ||
+      (rc = dev_alloc(&h->nb_start, 27 * (size_t)n + 32)) ||  // + 32: any 5-bit cell index stays inside
       (rc = dev_alloc(&h->cell_list, n)) || (rc = dev_alloc(&h->step_counters, kStepCounters)) ||
       (rc = dev_alloc(&h->keys, 2 * (size_t)n)) || (rc = dev_alloc(&h->vals, 2 * (size_t)n)) ||
       (rc = dev_alloc(&h->lookback, 4 * 256 * (size_t)h->ntiles)) ||
@@ -382,7 +454,8 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
       (rc = dev_alloc(&h->consts, nscenes)) || (rc = dev_alloc(&h->scene_h, nscenes)) ||
       (rc = dev_alloc(&h->meshes, nscenes)) || (rc = dev_alloc(&h->bbox, 6 * (size_t)nscenes)) ||
       (rc = dev_alloc(&h->ctl, kCtlWords)) || (rc = dev_alloc(&h->status, 1)) ||
-      (rc = dev_alloc(&h->capped, 1)) || (rc = dev_alloc(&h->aos_stage, 5 * (size_t)n)))
+      (rc = dev_alloc(&h->capped, 1)) || (rc = dev_alloc(&h->aos_stage, 5 * (size_t)n)) ||
+      (rc = dev_alloc(&h->pbar, 2)))
     return bail(rc);
   h->ci.mask = slots - 1;
   h->ci.shift = 32 - log2s;
@@ -401,6 +474,7 @@ int clsph_gpu_create_batched(const clsph_parameters* params, const clsph_kernel_
   for (uint32_t i = 0; i < n; ++i) iota[i] = i;
   if (cudaMemset(h->grids, 0, sizeof(DevGrid) * nscenes) != cudaSuccess ||
       cudaMemset(h->status, 0, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(h->pbar, 0, 2 * sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(h->capped, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemset(h->aux, 0, sizeof(float4) * n) != cudaSuccess ||
       cudaMemset(h->ncount, 0, sizeof(uint32_t) * n) != cudaSuccess ||
@@ -440,10 +514,11 @@ int clsph_gpu_destroy(clsph_gpu* h) {
     cudaFree(h->ids[s]);
   }
   void* bufs[] = {h->aux,      h->acc,      h->frec,      h->nlist,     h->ncount,      h->cell_list,
+                  h->nb_start,
                   h->step_counters, h->keys, h->vals,     h->lookback,    h->digit_total,
                   h->ci.keys,  h->ci.start, h->ci.end,    h->scene_of,    h->grids,
                   h->consts,   h->scene_h,  h->meshes,    h->bbox,        h->ctl,
-                  h->status,   h->capped,   h->aos_stage};
+                  h->status,   h->capped,   h->aos_stage, h->pbar};
   for (void* b : bufs) cudaFree(b);
   for (auto& m : h->scene_mesh) m.release();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -498,19 +573,51 @@ int clsph_gpu_set_scene_mesh(clsph_gpu* h, uint32_t scene, const float* normals,
     dm.vertices = sm.vertices;
     dm.indices = sm.indices;
     dm.faces = faces;
-    std::vector<uint32_t> start, list;
-    rc = build_face_grid(h->params[scene], vertices, vertex_count, indices, faces, start, list, dm);
+    FaceGridPlan plan{};
+    float reach = 0.f;
+    rc = plan_face_grid(h->params[scene], vertices, vertex_count, indices, faces, plan, reach);
     if (rc >= 256) return rc;
-    if (rc == 0) {
-      if ((rc = dev_alloc(&sm.cell_start, start.size())) || (rc = dev_alloc(&sm.cell_faces, list.size())))
-        return rc;
-      CUDA_TRY(cudaMemcpy(sm.cell_start, start.data(), sizeof(uint32_t) * start.size(), cudaMemcpyHostToDevice));
-      CUDA_TRY(cudaMemcpy(sm.cell_faces, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice));
+    if (rc == 0) {  // (a non-finite mesh keeps no lists: every face is scanned)
+      if ((rc = build_face_lists(h, sm, faces, plan))) return rc;
       dm.cell_start = sm.cell_start;
       dm.cell_faces = sm.cell_faces;
+      for (int a = 0; a < 3; ++a) {
+        dm.lo[a] = plan.glo[a];
+        dm.dims[a] = plan.dims[a];
+      }
+      dm.inv_cell = 1.f / plan.cell;
+      dm.reach = reach;
     }
   }
   return sync_scene_tables(h);
+}
+
+int clsph_gpu_read_face_lists(clsph_gpu* h, uint32_t scene, float* plan, uint32_t* cell_start,
+                              uint64_t start_cap, uint32_t* cell_faces, uint64_t faces_cap, uint32_t* sizes) {
+  if (!h || scene >= h->nscenes || !sizes) return fail(CLSPH_ERR_ARGUMENT, "read_face_lists: bad argument");
+  const SceneMesh& sm = h->scene_mesh[scene];
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (!sm.cell_start) {
+    sizes[0] = sizes[1] = 0;
+    return CLSPH_OK;
+  }
+  const FaceGridPlan& g = sm.plan;
+  sizes[0] = g.cells + 1;
+  sizes[1] = sm.list_len;
+  if (plan) {
+    const float v[10] = {g.glo[0], g.glo[1], g.glo[2], g.cell, g.pad, g.tol,
+                         (float)g.dims[0], (float)g.dims[1], (float)g.dims[2], h->mesh_host[scene].reach};
+    std::memcpy(plan, v, sizeof(v));
+  }
+  if (cell_start) {
+    if (start_cap < sizes[0]) return fail(CLSPH_ERR_ARGUMENT, "read_face_lists: start buffer too small");
+    CUDA_TRY(cudaMemcpy(cell_start, sm.cell_start, sizeof(uint32_t) * sizes[0], cudaMemcpyDeviceToHost));
+  }
+  if (cell_faces) {
+    if (faces_cap < sizes[1]) return fail(CLSPH_ERR_ARGUMENT, "read_face_lists: face buffer too small");
+    CUDA_TRY(cudaMemcpy(cell_faces, sm.cell_faces, sizeof(uint32_t) * sizes[1], cudaMemcpyDeviceToHost));
+  }
+  return CLSPH_OK;
 }
 
 int clsph_gpu_set_mesh(clsph_gpu* h, const float* normals, const float* vertices,
@@ -573,7 +680,13 @@ int clsph_gpu_step(clsph_gpu* h, uint32_t substeps) {
   if (!h) return fail(CLSPH_ERR_ARGUMENT, "step: null handle");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "step: upload particles first");
   uint32_t done = 0;
-  if (h->use_graph && !h->profiling && substeps >= 2) {
+  if (h->persistent && !h->profiling) {
+    int rc = launch_persistent(h, substeps);
+    if (rc) return rc;
+    h->substeps += substeps;
+    done = substeps;
+  }
+  if (h->use_graph && !h->profiling && substeps - done >= 2) {
     for (int kind = 1; kind >= 0; --kind) {  // the long graph first
       const uint32_t len = clsph_gpu::kGraphLen[kind];
       if (substeps - done < len) continue;
@@ -613,6 +726,12 @@ int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags) {
   uint32_t f = 0;
   CUDA_TRY(cudaMemcpy(&f, h->status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemset(h->status, 0, sizeof(uint32_t)));
+  if (f & kFlagBarrierStall) {
+    // the barrier words may be left mid-count: start the next launch afresh
+    CUDA_TRY(cudaMemset(h->pbar, 0, 2 * sizeof(uint32_t)));
+    return fail(CLSPH_ERR_CUDA, "sync: a grid barrier wait of the persistent substep kernel ran out "
+                                "(the substeps of that launch are incomplete)");
+  }
   if (f & kFlagSortStall)
     return fail(CLSPH_ERR_CUDA, "sync: a radix sort look-back wait ran out (that substep's order is wrong)");
   if (flags) *flags = f;
@@ -726,6 +845,8 @@ int clsph_gpu_kernel_times(clsph_gpu* h, int max_classes, char* names, int name_
   return CLSPH_OK;
 }
 
+static cudaEvent_t take_event_of(clsph_gpu* h) { return h->take_event(); }
+
 int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report_len) {
   if (!h || substeps == 0) return fail(CLSPH_ERR_ARGUMENT, "autotune: bad argument");
   if (!h->uploaded || h->partial) return fail(CLSPH_ERR_STATE, "autotune: upload particles first");
@@ -809,9 +930,47 @@ int clsph_gpu_autotune(clsph_gpu* h, uint32_t substeps, char* report, int report
     if (t < ta) { ta = t; best_a = a; }
   }
   h->advect_blocks_per_sm = best_a;
+  // whole substeps: CUDA-graph replays of the tuned launches against the
+  // persistent cooperative kernel; the faster form is kept
+  h->drop_graph();
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
+  bool use_persistent = false;
+  if (coop) {
+    const uint32_t even = std::max<uint32_t>(2u, substeps & ~1u);
+    const bool graph0 = h->use_graph;
+    cudaEvent_t e0 = take_event_of(h), e1 = take_event_of(h);
+    auto whole = [&](bool pers) -> double {
+      h->persistent = pers;
+      h->use_graph = true;
+      h->profiling = false;
+      cudaEventRecord(e0, h->stream);
+      const int rc = clsph_gpu_step(h, even);
+      cudaEventRecord(e1, h->stream);
+      cudaStreamSynchronize(h->stream);
+      float ms = 0.f;
+      const bool ok = rc == 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      save(true);
+      h->ids_sel = ids_sel0;
+      h->profiling = true;
+      return ok ? ms / even : 1e30;
+    };
+    whole(false);  // warm-up (graph capture)
+    const double tg = whole(false);
+    whole(true);
+    const double tp = whole(true);
+    use_persistent = tp < tg;
+    out += "whole substep: graph " + std::to_string(tg) + " ms, persistent " + std::to_string(tp) + " ms\n";
+    h->use_graph = graph0;
+    h->event_pool.push_back(e0);
+    h->event_pool.push_back(e1);
+    cudaGetLastError();
+  }
+  h->persistent = use_persistent;
   out += "chosen: density block " + std::to_string(best_d) + ", search " + std::to_string(best_s) +
          ", forces block " + std::to_string(best_f) +
-         ", advect blocks/SM " + std::to_string(best_a) + "\n";
+         ", advect blocks/SM " + std::to_string(best_a) +
+         (use_persistent ? ", persistent substeps" : ", launched substeps") + "\n";
   h->profiling = prof0;
   for (int k = 0; k < K_NUM_CLASSES; ++k) {
     h->class_ms[k] = 0.0;
@@ -860,6 +1019,26 @@ int clsph_gpu_set_wait_limits(clsph_gpu* h, uint32_t radix_lookback_spins, uint3
   h->mlp_wait_limit = mlp_wait_polls;
   h->radix_withheld_tile = radix_withheld_tile;
   h->drop_graph();  // the limits are kernel arguments of the captured launches
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_persistent(clsph_gpu* h, int enabled) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_persistent: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (enabled) {
+    int coop = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+    if (!coop) return fail(CLSPH_ERR_CUDA, "set_persistent: the device has no cooperative launch");
+  }
+  h->persistent = enabled != 0;
+  return CLSPH_OK;
+}
+
+int clsph_gpu_set_barrier_limits(clsph_gpu* h, uint32_t barrier_spins, uint32_t withheld_block) {
+  if (!h) return fail(CLSPH_ERR_ARGUMENT, "set_barrier_limits: null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->barrier_limit = barrier_spins;
+  h->withheld_block = withheld_block;
   return CLSPH_OK;
 }
 

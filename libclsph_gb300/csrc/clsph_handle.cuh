@@ -10,6 +10,8 @@
 
 #include "clsph_gpu.h"
 #include "clsph_kernels.cuh"
+#include "clsph_mesh.cuh"
+#include "clsph_persistent.cuh"
 
 using namespace clsph;
 
@@ -80,6 +82,8 @@ struct SceneMesh {
   uint32_t* indices = nullptr;
   uint32_t* cell_start = nullptr;
   uint32_t* cell_faces = nullptr;
+  FaceGridPlan plan{};    // grid of the per-cell triangle lists
+  uint32_t list_len = 0;  // entries in cell_faces
   void release() {
     cudaFree(normals);
     cudaFree(vertices);
@@ -123,7 +127,8 @@ struct clsph_gpu {
   float4* aux = nullptr;  // (rho, p, m/rho, p/rho^2)
   float4* acc = nullptr;
   float4* frec = nullptr;  // [2n] forces records: (pos, m/rho), (vel, p/rho^2)
-  uint32_t* nlist = nullptr;
+  uint16_t* nlist = nullptr;      // [nlist_cap][n] neighbour tags (visiting order)
+  uint32_t* nb_start = nullptr;   // [n][27] rows of the cells' neighbour starts (by first slot)
   uint32_t* ncount = nullptr;
   uint32_t nlist_cap = 64;
   uint32_t* cell_list = nullptr;      // first sorted slot of every occupied cell
@@ -144,6 +149,13 @@ struct clsph_gpu {
   int search = CLSPH_SEARCH_CELL_WARPS;  // neighbour search of the density kernel
   int forces_block = 128;
   uint32_t advect_blocks_per_sm = 8;
+
+  // the substep loop as one persistent cooperative launch (clsph_persistent.cuh)
+  bool persistent = false;
+  uint32_t* pbar = nullptr;         // grid barrier words
+  uint32_t persist_blocks = 0;      // co-resident blocks (0: not yet measured)
+  uint32_t barrier_limit = kBarrierSpins;
+  uint32_t withheld_block = kNoBlock;
 
   // bounds of the device waits (clsph_gpu_set_wait_limits)
   uint32_t radix_spin_limit = CLSPH_DEFAULT_LOOKBACK_SPINS;
@@ -238,6 +250,8 @@ namespace clsph_host {
 
 // Enqueues one substep up to and including `until` (CLSPH_STAGE_*).
 int enqueue_substep(clsph_gpu* h, int until);
+// Enqueues `substeps` whole substeps as persistent cooperative launches.
+int launch_persistent(clsph_gpu* h, uint32_t substeps);
 // Enqueues the advection of the sorted state (the CLSPH_STAGE_ADVECT part of
 // a substep) back into the resident buffers.
 int enqueue_advect(clsph_gpu* h);

@@ -2,8 +2,11 @@
 //
 // Data layout in HBM (SoA, sorted order, 16-byte float4 rows):
 //   pos[n], vel[n], ivel[n]   position, velocity, intermediate (half-step) velocity
-//   aux[n]                    (rho, p, m/rho, p/rho^2) of the substep
-//   nlist[cap][n], ncount[n]  contributing neighbours of each particle, in visiting order
+//   aux[n]                    (rho, p, own cell's first slot (bits), p/rho^2) of the substep
+//   nlist[cap][n], ncount[n]  contributing neighbours of each particle, in visiting order,
+//                             as 16-bit tags (neighbour cell k of 27 << 11 | offset in it)
+//   nb_start[n][27]           first slot of each of the 27 cells around a cell, in the
+//                             row of the cell's first slot (resolves the tags)
 //   acc[n]                    acceleration (forces -> advection)
 //   keys[2][n], vals[2][n]    radix-sort ping-pong (Morton key, source slot)
 //   ids[2][n]                 persistent particle ids (the reference has none)
@@ -187,11 +190,14 @@ __device__ __forceinline__ Window neighbour_window(float4 p, uint32_t key, const
 // Grid set-up of every scene (sph_simulation.cpp:199-252), one thread per
 // scene, from the bounding boxes accumulated by the previous kernel; resets
 // the boxes, the radix digit totals and the sort control for this substep.
-static __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
-                             const float* __restrict__ scene_h, uint32_t nscenes,
-                             uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
-                             uint32_t* __restrict__ step_counters, uint32_t* __restrict__ ctl) {
-  __shared__ uint32_t shift_s;
+// (The kernels of this file are thin wrappers around block-level bodies with
+// their shared memory passed in, so the persistent substep kernel of
+// clsph_persistent.cuh runs the same code on its own blocks.)
+__device__ __forceinline__ void grid_setup_block(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
+                                                 const float* __restrict__ scene_h, uint32_t nscenes,
+                                                 uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
+                                                 uint32_t* __restrict__ step_counters, uint32_t* __restrict__ ctl,
+                                                 uint32_t& shift_s) {
   for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) digit_total[i] = 0u;
   if (threadIdx.x < kStepCounters) step_counters[threadIdx.x] = 0u;
   if (threadIdx.x == 0) shift_s = 1u;
@@ -239,6 +245,14 @@ static __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __
   }
 }
 
+static __global__ void k_grid_setup(uint32_t* __restrict__ bbox_all, DevGrid* __restrict__ grids,
+                                    const float* __restrict__ scene_h, uint32_t nscenes,
+                                    uint32_t* __restrict__ status, uint32_t* __restrict__ digit_total,
+                                    uint32_t* __restrict__ step_counters, uint32_t* __restrict__ ctl) {
+  __shared__ uint32_t shift_s;
+  grid_setup_block(bbox_all, grids, scene_h, nscenes, status, digit_total, step_counters, ctl, shift_s);
+}
+
 static __global__ void k_bbox_reset(uint32_t* __restrict__ bbox, uint32_t nscenes) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < 6 * nscenes; k += gridDim.x * blockDim.x)
     bbox[k] = (k % 6) < 3 ? f2ord(2147483648.0f) : f2ord(-2147483648.0f);
@@ -257,8 +271,15 @@ __device__ __forceinline__ void bbox_atomics(const float v[6], uint32_t* bbox) {
   if (v[5] == v[5]) atomicMax(&bbox[5], f2ord(v[5]));
 }
 
-__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene, uint32_t* bbox_all) {
-  __shared__ int block_scene;
+struct BboxSmem {
+  int block_scene;
+  float red[6][kBlock / 32];
+};
+
+__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene, uint32_t* bbox_all,
+                                                BboxSmem& sm) {
+  int& block_scene = sm.block_scene;
+  auto& red = sm.red;
   if (threadIdx.x == 0) block_scene = -2;
   __syncthreads();
   if (scene >= 0) atomicCAS(&block_scene, -2, scene);
@@ -272,7 +293,6 @@ __device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene,
   }
   if (s0 < 0) return;
   uint32_t* bbox = bbox_all + 6 * (size_t)s0;
-  __shared__ float red[6][kBlock / 32];
   float v[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
@@ -304,6 +324,11 @@ __device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene,
       }
     }
   }
+}
+
+__device__ __forceinline__ void bbox_accumulate(float3 lo, float3 hi, int scene, uint32_t* bbox_all) {
+  __shared__ BboxSmem sm;
+  bbox_accumulate(lo, hi, scene, bbox_all, sm);
 }
 
 // Host AoS (80-byte particle records, 5 float4 each) -> SoA state, with
@@ -372,15 +397,14 @@ static __global__ void k_pack_aos(float4* __restrict__ aos, uint32_t n, State st
 }
 
 // Morton key per particle (grid.cl:56-66) and the largest key.
-static __global__ void __launch_bounds__(kBlock)
-    k_keys(const float4* __restrict__ pos, uint32_t n, const DevGrid* __restrict__ grids,
-           const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
-           uint32_t* __restrict__ keys) {
+__device__ __forceinline__ void keys_block(uint32_t vb, const float4* __restrict__ pos, uint32_t n,
+                                           const DevGrid* __restrict__ grids,
+                                           const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
+                                           uint32_t* __restrict__ keys, uint32_t& block_max) {
   const KeySplit split{ctl[kCtlShift]};
-  __shared__ uint32_t block_max;
   if (threadIdx.x == 0) block_max = 0u;
   __syncthreads();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = vb * blockDim.x + threadIdx.x;
   uint32_t key = 0u;
   if (i < n) {
     const uint32_t sc = scene_of[i];
@@ -396,6 +420,14 @@ static __global__ void __launch_bounds__(kBlock)
   if ((threadIdx.x & 31) == 0) atomicMax(&block_max, key);
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(&ctl[kCtlMaxKey], block_max);
+}
+
+static __global__ void __launch_bounds__(kBlock)
+    k_keys(const float4* __restrict__ pos, uint32_t n, const DevGrid* __restrict__ grids,
+           const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
+           uint32_t* __restrict__ keys) {
+  __shared__ uint32_t block_max;
+  keys_block(blockIdx.x, pos, n, grids, scene_of, ctl, keys, block_max);
 }
 
 // ---------------------------------------------------------------- radix sort
@@ -439,14 +471,15 @@ __device__ __forceinline__ void st_relaxed_gpu(uint32_t* p, uint32_t v) {
 
 // Digit counts of every pass in one read of the keys (16-byte loads), and the
 // look-back words of this substep's passes cleared.
-static __global__ void __launch_bounds__(kRadixThreads)
-    k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ ctl,
-                 uint32_t* __restrict__ digit_total, uint32_t* __restrict__ lookback, uint32_t ntiles) {
-  __shared__ uint32_t hist[4][256];
+__device__ __forceinline__ void radix_hist_blocks(uint32_t blk, uint32_t nblk, const uint32_t* __restrict__ keys,
+                                                  uint32_t n, const uint32_t* __restrict__ ctl,
+                                                  uint32_t* __restrict__ digit_total,
+                                                  uint32_t* __restrict__ lookback, uint32_t ntiles,
+                                                  uint32_t (&hist)[4][256]) {
   const uint32_t passes = radix_passes(ctl[kCtlMaxKey]);
   for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) hist[i >> 8][i & 255] = 0u;
-  const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t gstride = (size_t)gridDim.x * blockDim.x;
+  const size_t gtid = (size_t)blk * blockDim.x + threadIdx.x;
+  const size_t gstride = (size_t)nblk * blockDim.x;
   const size_t words = (size_t)passes * ntiles * 256u;
   for (size_t i = gtid; i < words; i += gstride) lookback[i] = 0u;
   __syncthreads();
@@ -470,16 +503,33 @@ static __global__ void __launch_bounds__(kRadixThreads)
 }
 
 static __global__ void __launch_bounds__(kRadixThreads)
-    k_radix_onesweep(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
-                     int pass, const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ digit_total,
-                     uint32_t* __restrict__ lookback, uint32_t ntiles, uint32_t* __restrict__ tile_ticket,
-                     uint32_t* __restrict__ status, uint32_t spin_limit, uint32_t withheld_tile) {
-  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
-  __shared__ uint32_t cnt[kRadixWarps][256];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t tile_off[256];
-  __shared__ uint32_t warp_sums[kRadixWarps];
-  __shared__ uint32_t tile_s;
+    k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ ctl,
+                 uint32_t* __restrict__ digit_total, uint32_t* __restrict__ lookback, uint32_t ntiles) {
+  __shared__ uint32_t hist[4][256];
+  radix_hist_blocks(blockIdx.x, gridDim.x, keys, n, ctl, digit_total, lookback, ntiles, hist);
+}
+
+struct RadixSmem {
+  uint32_t cnt[kRadixWarps][256];
+  uint32_t hist[256];
+  uint32_t tile_off[256];
+  uint32_t warp_sums[kRadixWarps];
+  uint32_t tile_s;
+};
+
+// One tile of one radix pass: takes the next tile number from the ticket;
+// returns false (the whole block) once every tile of the pass is taken.
+__device__ __forceinline__ bool radix_sweep_tile(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base,
+                                                 uint32_t n, int pass, const uint32_t* __restrict__ digit_total,
+                                                 uint32_t* __restrict__ lookback, uint32_t ntiles,
+                                                 uint32_t* __restrict__ tile_ticket, uint32_t* __restrict__ status,
+                                                 uint32_t spin_limit, uint32_t withheld_tile, RadixSmem& sm) {
+  auto& cnt = sm.cnt;
+  auto& hist = sm.hist;
+  auto& tile_off = sm.tile_off;
+  auto& warp_sums = sm.warp_sums;
+  uint32_t& tile_s = sm.tile_s;
+  __syncthreads();  // the block's previous tile is done with the shared arrays
   const uint32_t* keys_in = keys_base + (size_t)(pass & 1) * n;
   uint32_t* keys_out = keys_base + (size_t)((pass + 1) & 1) * n;
   const uint32_t* vals_in = vals_base + (size_t)(pass & 1) * n;
@@ -490,6 +540,7 @@ static __global__ void __launch_bounds__(kRadixThreads)
   hist[threadIdx.x] = 0u;
   __syncthreads();
   const uint32_t tile = tile_s;
+  if (tile >= ntiles) return false;
   const int shift = 8 * pass;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t base = tile * kRadixTile + warp * kRadixWarpSpan;
@@ -588,6 +639,18 @@ static __global__ void __launch_bounds__(kRadixThreads)
     keys_out[dst] = key[r];
     vals_out[dst] = val[r];
   }
+  return true;
+}
+
+static __global__ void __launch_bounds__(kRadixThreads)
+    k_radix_onesweep(uint32_t* __restrict__ keys_base, uint32_t* __restrict__ vals_base, uint32_t n,
+                     int pass, const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ digit_total,
+                     uint32_t* __restrict__ lookback, uint32_t ntiles, uint32_t* __restrict__ tile_ticket,
+                     uint32_t* __restrict__ status, uint32_t spin_limit, uint32_t withheld_tile) {
+  if ((uint32_t)pass >= radix_passes(ctl[kCtlMaxKey])) return;
+  __shared__ RadixSmem sm;
+  radix_sweep_tile(keys_base, vals_base, n, pass, digit_total, lookback, ntiles, tile_ticket, status,
+                   spin_limit, withheld_tile, sm);
 }
 
 // Gathers the state into sorted order (the stable scatter of sort.cl:41-59)
@@ -595,17 +658,22 @@ static __global__ void __launch_bounds__(kRadixThreads)
 // table of sph_simulation.cpp:162-170 in compact form).
 // Cell starts join the cell list with one atomic per block (slot order is
 // kept within the block, so the list stays close to sorted order).
-static __global__ void __launch_bounds__(kBlock)
-    k_gather(uint32_t n, const DevGrid* __restrict__ grids,
-             const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
-             const uint32_t* __restrict__ keys_base,
-             const uint32_t* __restrict__ vals_base, State src, State dst,
-             const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
-             CellIndex ci, uint32_t* __restrict__ cell_list,
-             uint32_t* __restrict__ cell_count) {
-  __shared__ uint32_t warp_base[kBlock / 32];
-  __shared__ uint32_t block_base;
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+struct GatherSmem {
+  uint32_t warp_base[kBlock / 32];
+  uint32_t block_base;
+};
+
+__device__ __forceinline__ void gather_block(uint32_t vb, uint32_t n, const DevGrid* __restrict__ grids,
+                                             const uint16_t* __restrict__ scene_of,
+                                             const uint32_t* __restrict__ ctl,
+                                             const uint32_t* __restrict__ keys_base,
+                                             const uint32_t* __restrict__ vals_base, State src, State dst,
+                                             const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
+                                             CellIndex ci, uint32_t* __restrict__ cell_list,
+                                             uint32_t* __restrict__ cell_count, GatherSmem& sm) {
+  auto& warp_base = sm.warp_base;
+  uint32_t& block_base = sm.block_base;
+  const uint32_t s = vb * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const KeySplit split{ctl[kCtlShift]};
   const uint32_t sel = sorted_sel(ctl[kCtlMaxKey]);
@@ -645,6 +713,20 @@ static __global__ void __launch_bounds__(kBlock)
   }
   __syncthreads();
   if (first) cell_list[block_base + warp_base[warp] + __popc(bal & ((1u << lane) - 1u))] = s;
+  __syncthreads();  // the shared counts are read before the block's next use
+}
+
+static __global__ void __launch_bounds__(kBlock)
+    k_gather(uint32_t n, const DevGrid* __restrict__ grids,
+             const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
+             const uint32_t* __restrict__ keys_base,
+             const uint32_t* __restrict__ vals_base, State src, State dst,
+             const uint32_t* __restrict__ ids_src, uint32_t* __restrict__ ids_dst,
+             CellIndex ci, uint32_t* __restrict__ cell_list,
+             uint32_t* __restrict__ cell_count) {
+  __shared__ GatherSmem sm;
+  gather_block(blockIdx.x, n, grids, scene_of, ctl, keys_base, vals_base, src, dst, ids_src, ids_dst, ci,
+               cell_list, cell_count, sm);
 }
 
 // ------------------------------------------------- density and forces
@@ -778,21 +860,62 @@ __device__ __forceinline__ uint32_t facing_mask(int ox, int oy, int oz) {
   return m;
 }
 
-template <class F>
+// Neighbour-list tags: the neighbour's cell as its index k < 27 among the 27
+// cells around the particle's own cell (z, y, x order, 13 = own) in bits
+// 11-15 and its offset in that cell in bits 0-10; a cell of 2048 or more
+// particles cannot be tagged (kNoTag) and sends its particles to the rescan.
+constexpr uint32_t kTagOffBits = 11;
+constexpr uint32_t kNoTag = 0xFFFFu;
+__device__ __forceinline__ uint32_t nb_tag(uint32_t k, uint32_t off) {
+  return off < (1u << kTagOffBits) ? (k << kTagOffBits) | off : kNoTag;
+}
+
+// Calls f(j, pj, tag) for every candidate of the window that faces the
+// particle's cell, in the reference's order, and g(k, start) once per window
+// cell before its candidates.
+template <class F, class G>
 __device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint32_t key,
                                                           uint32_t sbits, const CellIndex& ci,
-                                                          const float4* __restrict__ pos, F&& f) {
+                                                          const float4* __restrict__ pos, F&& f,
+                                                          G&& g) {
   const int c[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
   for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
     for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
       for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
-        const uint32_t need = facing_mask((int)x - c[0], (int)y - c[1], (int)z - c[2]);
+        const int ox = (int)x - c[0], oy = (int)y - c[1], oz = (int)z - c[2];
+        const uint32_t need = facing_mask(ox, oy, oz);
+        const uint32_t k = (uint32_t)((oz + 1) * 9 + (oy + 1) * 3 + (ox + 1));
         const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
+        g(k, r.x);
         for (uint32_t j = r.x; j < r.y; ++j) {
           const float4 pj = __ldg(&pos[j]);
-          if ((__float_as_uint(pj.w) & need) == need) f(j, pj);
+          if ((__float_as_uint(pj.w) & need) == need) f(j, pj, nb_tag(k, j - r.x));
         }
       }
+}
+template <class F>
+__device__ __forceinline__ void for_each_facing_candidate(const Window& w, uint32_t key,
+                                                          uint32_t sbits, const CellIndex& ci,
+                                                          const float4* __restrict__ pos, F&& f) {
+  for_each_facing_candidate(w, key, sbits, ci, pos, f, [](uint32_t, uint32_t) {});
+}
+
+// Per-particle outputs of the density pass: aux = (rho, p, first slot of the
+// particle's own cell as bits, p/rho^2) (the forces kernel resolves the
+// neighbour tags through that cell's nb_start row), the forces kernel's two
+// 16-byte neighbour records (position, m/rho) and (velocity, p/rho^2), and the
+// neighbour count (> nlist_cap: the list is incomplete or holds an untaggable
+// neighbour, so the forces kernel searches again).
+__device__ __forceinline__ void density_outputs(uint32_t i, uint32_t n, float rho, const Consts& c,
+                                                uint32_t own_start, float4 pi, const float4* __restrict__ vel,
+                                                float4* __restrict__ aux_out, float4* __restrict__ frec,
+                                                uint32_t* __restrict__ ncount, uint32_t count) {
+  const float4 a = density_aux(rho, c);
+  aux_out[i] = make_float4(a.x, a.y, __uint_as_float(own_start), a.w);
+  const float4 v = vel[i];
+  frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
+  frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
+  ncount[i] = count;
 }
 
 template <int BLOCK>
@@ -801,9 +924,10 @@ __global__ void __launch_bounds__(BLOCK)
               const uint32_t* __restrict__ ctl,
               const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos, CellIndex ci,
               const Consts* __restrict__ consts, float4* __restrict__ aux_out,
-              uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap,
-              const float4* __restrict__ vel, float4* __restrict__ frec) {
-  __shared__ uint32_t cand[kScanCap][BLOCK];
+              uint16_t* __restrict__ nlist, uint32_t* __restrict__ ncount, uint32_t nlist_cap,
+              const float4* __restrict__ vel, float4* __restrict__ frec, uint32_t* __restrict__ nb_start) {
+  __shared__ uint16_t cand[kScanCap][BLOCK];  // tags of the cull's survivors
+  __shared__ uint32_t cstart[27][BLOCK];      // first slot of each window cell
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const KeySplit split{ctl[kCtlShift]};
@@ -816,82 +940,131 @@ __global__ void __launch_bounds__(BLOCK)
   const Window w = neighbour_window(pi, key, grids[sc]);
   const float hh = XMUL(c.h, c.h);
   uint32_t found = 0;
-  for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) {
-      if (found < kScanCap) cand[found][threadIdx.x] = j;
-      ++found;
-    }
-  });
+  for_each_facing_candidate(
+      w, key, sbits, ci, pos,
+      [&](uint32_t, float4 pj, uint32_t tag) {
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) {
+          if (found < kScanCap) cand[found][threadIdx.x] = (uint16_t)tag;
+          found = tag == kNoTag ? kScanCap + 1u : found + 1u;  // untaggable: rescan
+        }
+      },
+      [&](uint32_t k, uint32_t start) { cstart[k][threadIdx.x] = start; });
+  const uint32_t own_start = cstart[13][threadIdx.x];
   float rho = 0.f;
   uint32_t kept = 0;
-  auto visit = [&](uint32_t j, float4 pj) {
+  bool untagged = false;
+  auto visit = [&](uint32_t j, float4 pj, uint32_t tag) {
     const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
     const float rr = xnorm(d);
     if (rr < c.h) {
       rho = XADD(rho, poly6_term(rr, hh, c));
-      if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], j);
+      if (tag == kNoTag) untagged = true;
+      else if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], (uint16_t)tag);
       ++kept;
     }
   };
   if (found <= (uint32_t)kScanCap) {
     for (uint32_t k = 0; k < found; ++k) {
-      const uint32_t j = cand[k][threadIdx.x];
-      visit(j, __ldg(&pos[j]));
+      const uint32_t tag = cand[k][threadIdx.x];
+      const uint32_t j = cstart[tag >> kTagOffBits][threadIdx.x] + (tag & ((1u << kTagOffBits) - 1u));
+      visit(j, __ldg(&pos[j]), tag);
     }
   } else {
-    for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
+    for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj, uint32_t tag) {
       const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj);
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= c.cull_r2) visit(j, pj, tag);
     });
   }
-  const float4 a = density_aux(rho, c);
-  aux_out[i] = a;
-  // the forces kernel's per-neighbour record: (position, m/rho), (velocity, p/rho^2)
-  const float4 v = vel[i];
-  frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
-  frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
-  ncount[i] = kept;  // > nlist_cap: the list is incomplete, forces search again
+  // the own cell's row of the neighbour-start table (every particle of the
+  // cell writes the same values for the cells of its window)
+  const int cc[3] = {(int)compact_bits3(key), (int)compact_bits3(key >> 1), (int)compact_bits3(key >> 2)};
+  for (uint32_t z = w.lo[2]; z <= w.hi[2]; ++z)
+    for (uint32_t y = w.lo[1]; y <= w.hi[1]; ++y)
+      for (uint32_t x = w.lo[0]; x <= w.hi[0]; ++x) {
+        const uint32_t k = (uint32_t)(((int)z - cc[2] + 1) * 9 + ((int)y - cc[1] + 1) * 3 + ((int)x - cc[0] + 1));
+        nb_start[(size_t)own_start * 27u + k] = cstart[k][threadIdx.x];
+      }
+  density_outputs(i, n, rho, c, own_start, pi, vel, aux_out, frec, ncount,
+                  untagged ? max(kept, nlist_cap + 1u) : kept);
 }
 
 // ------------------------------------------------- density, one warp per cell
 // The warp takes one occupied cell at a time (dynamic work counter), looks up
 // the 27 cells around it once (lane k < 27: offset k in the reference's z, y,
-// x loop order) and holds the cell's particles, two per lane. For each
-// neighbour cell, in that order, that lies in at least one particle's window,
-// it stages the cell's candidates that face the own cell (the far half is
-// skipped by half code), 32 at a time and compacted by ballot, which keeps
-// their sorted order, in shared memory. Every lane then tests its particles
-// against the staged candidates (broadcast reads) and appends the survivors to
-// the particle's buffer, so each buffer holds the reference's visiting order.
-// The survivors are then evaluated exactly per particle, as in k_density.
-// A buffer entry is (window cell << 11) | offset in that cell; cells of 2048
-// or more particles and full buffers send the particle to the in-order rescan.
-// This form runs at 64 registers and 27 KB of shared memory per block of 4
-// warps, 8 resident blocks per SM; variants that needed more registers (a
-// packed f32x2 or TF32 tensor-core cull, 64-slot chunks, x-half slot pairs)
-// or forced fewer (a 56-register cap) measured slower.
+// x loop order; also stored as the cell's nb_start row) and holds the cell's
+// particles, two per lane. For each neighbour cell, in that order, that lies
+// in at least one particle's window, it stages the cell's candidates that face
+// the own cell (the far half is skipped by half code), 32 at a time and
+// compacted by ballot, which keeps their sorted order, in shared memory, with
+// coordinates relative to the own cell's centre and their negated squared
+// norm. A lane tests its particles against each staged candidate with three
+// FMAs, 2 p'.q' - |q'|^2 >= |p'|^2 - R^2 (the squared distance with the
+// particle's part precomputed), sets the candidate's bit in a per-chunk hit
+// mask, and after the chunk appends the hits' tags to the particle's buffer
+// in bit order, so each buffer holds the reference's visiting order. The
+// survivors are then evaluated exactly per particle, as in k_density.
+//
+// Rounding of the cull: cell-relative coordinates are within 3h of the
+// centre, so every intermediate of the test is below 50 h^2 and the four
+// roundings of each side stay below 3e-5 h^2, a fifth of the cull's margin
+// (R^2 = 1.0005 h^2); the test is conservative, and the exact evaluation
+// decides.
+// A buffer entry is a neighbour tag; cells of 2048 or more particles and full
+// buffers send the particle to the in-order rescan.
 constexpr int kCellWarps = 4;
-constexpr uint32_t kCellOffBits = 11;
+constexpr uint32_t kCellOffBits = kTagOffBits;
+
+// Per neighbour offset k (z, y, x order): the half-code bits an own particle
+// needs to face that cell (low 6 bits) and the bits a candidate of that cell
+// needs to face the own cell (next 6 bits), facing_mask(-o) | facing_mask(o) << 6.
+struct OffsetMasks {
+  uint16_t m[27];
+};
+constexpr OffsetMasks make_offset_masks() {
+  OffsetMasks t{};
+  for (int k = 0; k < 27; ++k) {
+    const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+    uint32_t own = 0, cand = 0;
+    for (int a = 0; a < 3; ++a) {
+      if (o[a] < 0) { own |= 1u << (2 * a); cand |= 2u << (2 * a); }
+      if (o[a] > 0) { own |= 2u << (2 * a); cand |= 1u << (2 * a); }
+    }
+    t.m[k] = (uint16_t)(own | (cand << 6));
+  }
+  return t;
+}
+__constant__ OffsetMasks kOffsetMasks = make_offset_masks();
 
 __device__ __forceinline__ bool near_cull(const float4& p, const float4& q, float r2) {
   const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2;
 }
 
+// survivor buffer per particle: 48 tags (40 with 8 warps, which keeps the
+// block within 48 KB of shared memory); fuller ones rescan
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_density_cells(uint32_t n, const DevGrid* __restrict__ grids,
-                    const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
-                    const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos,
-                    CellIndex ci, const Consts* __restrict__ consts, float4* __restrict__ aux_out,
-                    uint32_t* __restrict__ nlist, uint32_t* __restrict__ ncount,
-                    uint32_t nlist_cap, const float4* __restrict__ vel,
-                    float4* __restrict__ frec, const uint32_t* __restrict__ cell_list,
-                    uint32_t* __restrict__ counters) {
-  __shared__ uint4 stage[WARPS][32];
-  __shared__ uint32_t starts[WARPS][32];
-  __shared__ uint16_t cand[WARPS][kScanCap][64];
+struct DensitySmem {
+  static constexpr uint32_t kCap = WARPS >= 8 ? 40u : (uint32_t)kScanCap;
+  float4 stage[WARPS][32];
+  uint32_t stag[WARPS][32];
+  uint32_t starts[WARPS][32];
+  uint16_t cand[WARPS][kCap][64];
+};
+
+template <int WARPS>
+__device__ __forceinline__ void density_cells_warps(
+    uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+    const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos,
+    CellIndex ci, const Consts* __restrict__ consts, float4* __restrict__ aux_out, uint16_t* __restrict__ nlist,
+    uint32_t* __restrict__ ncount, uint32_t nlist_cap, const float4* __restrict__ vel,
+    float4* __restrict__ frec, const uint32_t* __restrict__ cell_list, uint32_t* __restrict__ counters,
+    uint32_t* __restrict__ nb_start, DensitySmem<WARPS>& sm) {
+  constexpr uint32_t kCap = DensitySmem<WARPS>::kCap;
+  auto& stage = sm.stage;
+  auto& stag = sm.stag;
+  auto& starts = sm.starts;
+  auto& cand = sm.cand;
   const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t ncells = counters[kCntCells];
@@ -908,12 +1081,17 @@ __global__ void __launch_bounds__(WARPS * 32)
     const uint32_t sbits = split.scene_bits(sc);
     const uint32_t cx = compact_bits3(key), cy = compact_bits3(key >> 1), cz = compact_bits3(key >> 2);
     const float cull_r2 = consts[sc].cull_r2;
+    const DevGrid& gr = grids[sc];
+    // the own cell's centre: the origin of the cull's coordinates
+    const float ox = gr.lo[0] + ((float)cx + 0.5f) * gr.cell, oy = gr.lo[1] + ((float)cy + 0.5f) * gr.cell,
+                oz = gr.lo[2] + ((float)cz + 0.5f) * gr.cell;
     uint32_t nb_s = 0, nb_e = 0;
     if (lane < 27u) {
       const uint32_t x = cx + lane % 3u - 1u, y = cy + (lane / 3u) % 3u - 1u, z = cz + lane / 9u - 1u;
       const uint2 r = cell_lookup(ci, morton3(x, y, z) | sbits);
       nb_s = r.x;
       nb_e = r.y;
+      nb_start[(size_t)s0 * 27u + lane] = nb_s;
     }
     starts[wid][lane] = nb_s;
     __syncwarp();
@@ -926,15 +1104,23 @@ __global__ void __launch_bounds__(WARPS * 32)
       const float4 pb = vb ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
       const uint32_t code_a = __float_as_uint(pa.w), code_b = __float_as_uint(pb.w);
       const bool two = __any_sync(0xFFFFFFFFu, vb);
-      uint32_t fa = wide ? kScanCap + 1u : 0u, fb = fa;
+      // 2 p' and |p'|^2 - R^2 of both particles
+      const float ax = pa.x - ox, ay = pa.y - oy, az = pa.z - oz;
+      const float bx = pb.x - ox, by = pb.y - oy, bz = pb.z - oz;
+      const float a2x = 2.f * ax, a2y = 2.f * ay, a2z = 2.f * az;
+      const float b2x = 2.f * bx, b2y = 2.f * by, b2z = 2.f * bz;
+      const float ta = fmaf(ax, ax, fmaf(ay, ay, az * az)) - cull_r2;
+      const float tb = fmaf(bx, bx, fmaf(by, by, bz * bz)) - cull_r2;
+      uint32_t fa = wide ? kCap + 1u : 0u, fb = fa;
       for (uint32_t k = 0; k < 27u && !wide; ++k) {
-        const int ox = (int)(k % 3u) - 1, oy = (int)((k / 3u) % 3u) - 1, oz = (int)(k / 9u) - 1;
-        const uint32_t need = facing_mask(-ox, -oy, -oz);  // the own particle's half toward the cell
+        const uint32_t masks = kOffsetMasks.m[k];
+        const uint32_t need = masks & 63u;  // the own particle's half toward the cell
+        const uint32_t fm = masks >> 6;     // a candidate's half toward the own cell
         const bool na = va && (code_a & need) == need;
         const bool nb = vb && (code_b & need) == need;
         if (!__any_sync(0xFFFFFFFFu, na || nb)) continue;
+        const float tak = na ? ta : INFINITY, tbk = nb ? tb : INFINITY;
         const uint32_t s = __shfl_sync(0xFFFFFFFFu, nb_s, k), e = __shfl_sync(0xFFFFFFFFu, nb_e, k);
-        const uint32_t fm = facing_mask(ox, oy, oz);
         for (uint32_t cb = s; cb < e; cb += 32u) {
           const uint32_t j = cb + lane;
           float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -944,25 +1130,41 @@ __global__ void __launch_bounds__(WARPS * 32)
             f = (__float_as_uint(q.w) & fm) == fm;
           }
           const uint32_t bal = __ballot_sync(0xFFFFFFFFu, f);
-          const uint32_t tagj = (k << kCellOffBits) | (j - s);
-          if (f)
-            stage[wid][__popc(bal & lt)] =
-                make_uint4(__float_as_uint(q.x), __float_as_uint(q.y), __float_as_uint(q.z), tagj);
-          __syncwarp();
           const uint32_t cnt = __popc(bal);
-          for (uint32_t t = 0; t < cnt; ++t) {
-            const uint4 r = stage[wid][t];
-            const float4 rq = make_float4(__uint_as_float(r.x), __uint_as_float(r.y), __uint_as_float(r.z), 0.f);
-            const bool hit_a = na && near_cull(pa, rq, cull_r2);
-            const bool hit_b = two && nb && near_cull(pb, rq, cull_r2);
-            if (hit_a) {
-              if (fa < (uint32_t)kScanCap) cand[wid][fa][lane] = (uint16_t)r.w;
-              ++fa;
+          if (f) {
+            const uint32_t at = __popc(bal & lt);
+            const float qx = q.x - ox, qy = q.y - oy, qz = q.z - oz;
+            stage[wid][at] = make_float4(qx, qy, qz, -fmaf(qx, qx, fmaf(qy, qy, qz * qz)));
+            stag[wid][at] = (k << kCellOffBits) | (j - s);
+          }
+          // slots [cnt, 8 * ceil(cnt / 8)) hold a candidate no test accepts
+          if (cnt + lane < ((cnt + 7u) & ~7u)) stage[wid][cnt + lane] = make_float4(0.f, 0.f, 0.f, -INFINITY);
+          __syncwarp();
+          uint32_t ma = 0, mb = 0;
+          // eight candidates per step, each with its own constant bit
+          for (uint32_t t0 = 0; t0 < cnt; t0 += 8u) {
+            uint32_t ga = 0, gb = 0;
+#pragma unroll
+            for (uint32_t u = 0; u < 8u; ++u) {
+              const float4 r = stage[wid][t0 + u];
+              if (fmaf(a2x, r.x, fmaf(a2y, r.y, fmaf(a2z, r.z, r.w))) >= tak) ga |= 1u << u;
+              if (two && fmaf(b2x, r.x, fmaf(b2y, r.y, fmaf(b2z, r.z, r.w))) >= tbk) gb |= 1u << u;
             }
-            if (hit_b) {
-              if (fb < (uint32_t)kScanCap) cand[wid][fb][lane + 32u] = (uint16_t)r.w;
-              ++fb;
-            }
+            ma |= ga << t0;
+            mb |= gb << t0;
+          }
+          // hits in candidate order
+          while (ma) {
+            const uint32_t t = __ffs(ma) - 1u;
+            ma &= ma - 1u;
+            if (fa < kCap) cand[wid][fa][lane] = (uint16_t)stag[wid][t];
+            ++fa;
+          }
+          while (mb) {
+            const uint32_t t = __ffs(mb) - 1u;
+            mb &= mb - 1u;
+            if (fb < kCap) cand[wid][fb][lane + 32u] = (uint16_t)stag[wid][t];
+            ++fb;
           }
           __syncwarp();
         }
@@ -972,33 +1174,31 @@ __global__ void __launch_bounds__(WARPS * 32)
         const float hh = XMUL(c.h, c.h);
         float rho = 0.f;
         uint32_t kept = 0;
-        auto visit = [&](uint32_t j, float4 pj) {
+        bool untagged = false;
+        auto visit = [&](uint32_t j, float4 pj, uint32_t tag) {
           const V3 d = {XSUB(pi.x, pj.x), XSUB(pi.y, pj.y), XSUB(pi.z, pj.z)};
           const float rr = xnorm(d);
           if (rr < c.h) {
             rho = XADD(rho, poly6_term(rr, hh, c));
-            if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], j);
+            if (tag == kNoTag) untagged = true;
+            else if (kept < nlist_cap) __stcs(&nlist[(size_t)kept * n + i], (uint16_t)tag);
             ++kept;
           }
         };
-        if (found <= (uint32_t)kScanCap) {
+        if (found <= kCap) {
           for (uint32_t k = 0; k < found; ++k) {
             const uint32_t tag = cand[wid][k][col];
             const uint32_t j = starts[wid][tag >> kCellOffBits] + (tag & ((1u << kCellOffBits) - 1u));
-            visit(j, __ldg(&pos[j]));
+            visit(j, __ldg(&pos[j]), tag);
           }
         } else {
           const Window w = neighbour_window(pi, key, grids[sc]);
-          for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj) {
-            if (near_cull(pi, pj, c.cull_r2)) visit(j, pj);
+          for_each_facing_candidate(w, key, sbits, ci, pos, [&](uint32_t j, float4 pj, uint32_t tag) {
+            if (near_cull(pi, pj, c.cull_r2)) visit(j, pj, tag);
           });
         }
-        const float4 a = density_aux(rho, c);
-        aux_out[i] = a;
-        const float4 v = vel[i];
-        frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
-        frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
-        ncount[i] = kept;
+        density_outputs(i, n, rho, c, s0, pi, vel, aux_out, frec, ncount,
+                        untagged ? max(kept, nlist_cap + 1u) : kept);
       };
       if (va) finish(ia, pa, fa, lane);
       if (vb) finish(ib, pb, fb, lane + 32u);
@@ -1006,6 +1206,21 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
     __syncwarp();
   }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_density_cells(uint32_t n, const DevGrid* __restrict__ grids,
+                    const uint16_t* __restrict__ scene_of, const uint32_t* __restrict__ ctl,
+                    const uint32_t* __restrict__ keys_base, const float4* __restrict__ pos,
+                    CellIndex ci, const Consts* __restrict__ consts, float4* __restrict__ aux_out,
+                    uint16_t* __restrict__ nlist, uint32_t* __restrict__ ncount,
+                    uint32_t nlist_cap, const float4* __restrict__ vel,
+                    float4* __restrict__ frec, const uint32_t* __restrict__ cell_list,
+                    uint32_t* __restrict__ counters, uint32_t* __restrict__ nb_start) {
+  __shared__ DensitySmem<WARPS> sm;
+  density_cells_warps<WARPS>(n, grids, scene_of, ctl, keys_base, pos, ci, consts, aux_out, nlist, ncount,
+                             nlist_cap, vel, frec, cell_list, counters, nb_start, sm);
 }
 
 
@@ -1023,9 +1238,9 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
     k_density_pwarp(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
                     const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ keys_base,
                     const float4* __restrict__ pos, CellIndex ci, const Consts* __restrict__ consts,
-                    float4* __restrict__ aux_out, uint32_t* __restrict__ nlist,
+                    float4* __restrict__ aux_out, uint16_t* __restrict__ nlist,
                     uint32_t* __restrict__ ncount, uint32_t nlist_cap, const float4* __restrict__ vel,
-                    float4* __restrict__ frec) {
+                    float4* __restrict__ frec, uint32_t* __restrict__ nb_start) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1043,6 +1258,7 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
   const float h = c.h, cull_r2 = c.cull_r2;
   float rho = 0.f;
   uint32_t kept = 0;
+  bool untagged = false;
   // lane k < 27 looks up window cell k (z, y, x order) in parallel
   uint32_t cs = 0, ce = 0;
   bool inw = false;
@@ -1056,6 +1272,8 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
       ce = r.y;
     }
   }
+  const uint32_t own_start = __shfl_sync(0xFFFFFFFFu, cs, 13);
+  if (inw) nb_start[(size_t)own_start * 27u + lane] = cs;  // the same values from every particle of the cell
   uint32_t cells = __ballot_sync(0xFFFFFFFFu, inw && ce > cs);
   while (cells) {
     const uint32_t k = __ffs(cells) - 1u;
@@ -1078,8 +1296,10 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
         }
       }
       uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+      const uint32_t tag = nb_tag(k, j - r.x);
+      untagged |= __any_sync(0xFFFFFFFFu, hit && tag == kNoTag);
       const uint32_t at = kept + __popc(bal & lt);
-      if (hit && at < nlist_cap) __stcs(&nlist[(size_t)at * n + i], j);
+      if (hit && at < nlist_cap) __stcs(&nlist[(size_t)at * n + i], (uint16_t)tag);
       kept += __popc(bal);
       while (bal) {  // in lane order: the reference's summation sequence
         const int l = __ffs(bal) - 1;
@@ -1088,14 +1308,9 @@ static __global__ void __launch_bounds__(kParticleWarps * 32)
       }
     }
   }
-  if (lane == 0) {
-    const float4 a = density_aux(rho, c);
-    aux_out[i] = a;
-    const float4 v = vel[i];
-    frec[i] = make_float4(pi.x, pi.y, pi.z, a.z);
-    frec[(size_t)n + i] = make_float4(v.x, v.y, v.z, a.w);
-    ncount[i] = kept;
-  }
+  if (lane == 0)
+    density_outputs(i, n, rho, c, own_start, pi, vel, aux_out, frec, ncount,
+                    untagged ? max(kept, nlist_cap + 1u) : kept);
 }
 
 // Per-pair hook of k_forces (the learned stepper gathers its neighbour
@@ -1109,16 +1324,14 @@ struct NoForceHook {
 
 // Internal forces (forces.cl:45-112) -> acceleration (sph.cl:53-58), walking
 // the neighbour list of k_density (or the window, for overflowing lists).
-template <int BLOCK, class Hook = NoForceHook>
-__global__ void __launch_bounds__(BLOCK)
-    k_forces(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
-             const uint32_t* __restrict__ ctl,
-             const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,
-             CellIndex ci, const Consts* __restrict__ consts, const uint32_t* __restrict__ nlist,
-             const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
-             float4* __restrict__ acc_out, Hook hook, const float4* __restrict__ frec) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+template <class Hook>
+__device__ __forceinline__ void forces_particle(
+    uint32_t i, uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+    const uint32_t* __restrict__ ctl, const uint32_t* __restrict__ keys_base, State st,
+    const float4* __restrict__ aux, CellIndex ci, const Consts* __restrict__ consts,
+    const uint16_t* __restrict__ nlist, const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
+    float4* __restrict__ acc_out, const Hook& hook, const float4* __restrict__ frec,
+    const uint32_t* __restrict__ nb_start) {
   typename Hook::Acc ha = hook.begin(i);
   const uint32_t sc = scene_of[i];
   const Consts c = consts[sc];
@@ -1143,20 +1356,33 @@ __global__ void __launch_bounds__(BLOCK)
   auto pair = [&](uint32_t j) { pair_with(j, __ldg(&frec[j]), __ldg(&frec[(size_t)n + j])); };
   const uint32_t cnt = ncount[i];
   if (cnt <= nlist_cap) {
-    // software pipeline: the list entry two pairs ahead and the records of
-    // the next pair are in flight while a pair is evaluated
+    // a tag names the neighbour's cell among the 27 around the own cell and
+    // its offset there; the own cell's nb_start row holds their first slots
+    const uint32_t* nbs = nb_start + (size_t)__float_as_uint(ai.z) * 27u;
+    auto slot = [&](uint32_t tag) {
+      return __ldg(&nbs[tag >> kTagOffBits]) + (tag & ((1u << kTagOffBits) - 1u));
+    };
+    // software pipeline: while a pair is evaluated, the tag three pairs
+    // ahead is loaded, the tag two ahead is resolved to its slot and the
+    // records of the next pair are loaded
     if (cnt > 0) {
-      uint32_t j = __ldcs(&nlist[i]);
-      uint32_t jn = cnt > 1 ? __ldcs(&nlist[(size_t)n + i]) : j;
+      auto tag_at = [&](uint32_t k) { return (uint32_t)__ldcs(&nlist[(size_t)k * n + i]); };
+      const uint32_t t0 = tag_at(0);
+      const uint32_t t1 = cnt > 1 ? tag_at(1) : t0;
+      uint32_t tnn = cnt > 2 ? tag_at(2) : t1;
+      uint32_t j = slot(t0);
+      uint32_t jn = slot(t1);
       float4 pj = __ldg(&frec[j]), sj = __ldg(&frec[(size_t)n + j]);
       for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t jnn = k + 2 < cnt ? __ldcs(&nlist[(size_t)(k + 2) * n + i]) : jn;
+        const uint32_t t3 = k + 3 < cnt ? tag_at(k + 3) : tnn;
+        const uint32_t jnn = slot(tnn);
         const float4 pn = __ldg(&frec[jn]), sn = __ldg(&frec[(size_t)n + jn]);
         pair_with(j, pj, sj);
         j = jn;
         jn = jnn;
         pj = pn;
         sj = sn;
+        tnn = t3;
       }
     }
   } else {
@@ -1174,6 +1400,21 @@ __global__ void __launch_bounds__(BLOCK)
   const float4 a = finish_accel(f, ai.x, c);
   acc_out[i] = a;
   hook.end(ha, i, a);
+}
+
+template <int BLOCK, class Hook = NoForceHook>
+__global__ void __launch_bounds__(BLOCK)
+    k_forces(uint32_t n, const DevGrid* __restrict__ grids, const uint16_t* __restrict__ scene_of,
+             const uint32_t* __restrict__ ctl,
+             const uint32_t* __restrict__ keys_base, State st, const float4* __restrict__ aux,
+             CellIndex ci, const Consts* __restrict__ consts, const uint16_t* __restrict__ nlist,
+             const uint32_t* __restrict__ ncount, uint32_t nlist_cap,
+             float4* __restrict__ acc_out, Hook hook, const float4* __restrict__ frec,
+             const uint32_t* __restrict__ nb_start) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  forces_particle(i, n, grids, scene_of, ctl, keys_base, st, aux, ci, consts, nlist, ncount, nlist_cap,
+                  acc_out, hook, frec, nb_start);
 }
 
 // ------------------------------------------------------- mesh collision
@@ -1280,16 +1521,16 @@ __device__ __forceinline__ float4 learned_correction(float4 y, const float* y_st
 }
 
 template <bool kLearned>
-__global__ void __launch_bounds__(kBlock, 4)
-    k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out,
-             const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
-             const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
-             uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count,
-             const float4* __restrict__ corr, float dt_mult, float pos_w, const float4* __restrict__ aux,
-             const float* __restrict__ y_stats) {
+__device__ __forceinline__ void advect_blocks(
+    uint32_t blk, uint32_t nblk, uint32_t n, State in, const float4* __restrict__ acc, State out,
+    const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
+    const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
+    uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count,
+    const float4* __restrict__ corr, float dt_mult, float pos_w, const float4* __restrict__ aux,
+    const float* __restrict__ y_stats, BboxSmem& bsm) {
   const float qnan = __int_as_float(0x7FC00000);
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+  const uint32_t stride = nblk * blockDim.x;
+  for (uint32_t base = blk * blockDim.x; base < n; base += stride) {
     const uint32_t i = base + threadIdx.x;
     float3 lo = make_float3(qnan, qnan, qnan), hi = lo;
     int scene = -1;
@@ -1360,8 +1601,22 @@ __global__ void __launch_bounds__(kBlock, 4)
     lo = make_float3(pos.x, pos.y, pos.z);
     hi = lo;
     }
-    bbox_accumulate(lo, hi, scene, bbox);
+    bbox_accumulate(lo, hi, scene, bbox, bsm);
+    __syncthreads();  // the shared reduction is read before the next chunk reuses it
   }
+}
+
+template <bool kLearned>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_advect(uint32_t n, State in, const float4* __restrict__ acc, State out,
+             const DevMesh* __restrict__ meshes, const Consts* __restrict__ consts,
+             const uint16_t* __restrict__ scene_of, uint32_t max_iters, uint32_t* __restrict__ bbox,
+             uint32_t* __restrict__ status, unsigned long long* __restrict__ capped_count,
+             const float4* __restrict__ corr, float dt_mult, float pos_w, const float4* __restrict__ aux,
+             const float* __restrict__ y_stats) {
+  __shared__ BboxSmem bsm;
+  advect_blocks<kLearned>(blockIdx.x, gridDim.x, n, in, acc, out, meshes, consts, scene_of, max_iters, bbox,
+                          status, capped_count, corr, dt_mult, pos_w, aux, y_stats, bsm);
 }
 
 // Dense reference cell table of one scene from the sorted keys of its slot

@@ -301,8 +301,9 @@ int launch_forces_hooked(clsph_gpu* h, const FeatureHook& hook) {
   auto go = [&](auto kernel) {
     h->launch(K_FEATURES, kernel, grid, dim3(b), h->n, (const DevGrid*)h->grids,
               (const uint16_t*)h->scene_of, (const uint32_t*)h->ctl, (const uint32_t*)h->keys, h->st[1],
-              (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint32_t*)h->nlist,
-              (const uint32_t*)h->ncount, h->nlist_cap, h->acc, hook, (const float4*)h->frec);
+              (const float4*)h->aux, h->ci, (const Consts*)h->consts, (const uint16_t*)h->nlist,
+              (const uint32_t*)h->ncount, h->nlist_cap, h->acc, hook, (const float4*)h->frec,
+              (const uint32_t*)h->nb_start);
   };
   if (b == 64) go(k_forces<64, FeatureHook>);
   else if (b == 256) go(k_forces<256, FeatureHook>);
@@ -391,6 +392,40 @@ int gemm(cudaStream_t s, const bf16* A, int lda, const bf16* B, int ldb, int M, 
   return 0;
 }
 
+// Training GEMMs on the tensor cores (clsph_nn::k_gemm_tc); timeouts of its
+// bounded waits set bit kTrainWaitBit of the network's error word.
+constexpr uint32_t kTrainWaitBit = 4u;
+
+template <int BN, bool A_K, bool B_K, class Epi>
+int gemm_tc(cudaStream_t s, uint32_t* err, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K,
+            int k_split, Epi epi) {
+  using L = clsph_nn::GemmTcLayout<BN>;
+  (void)sizeof(L);
+  if (N != BN || M % clsph_nn::kGtRows || k_split <= 0 || K % k_split || k_split % clsph_nn::kGtBK ||
+      lda % 8 || ldb % 8)
+    return fail(CLSPH_ERR_ARGUMENT, "mlp: GEMM shape not tileable");
+  auto kernel = clsph_nn::k_gemm_tc<BN, A_K, B_K, Epi>;
+  // set on every launch: the attribute belongs to the current device
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clsph_nn::kGtSmem);
+  if (e != cudaSuccess) return fail(CLSPH_ERR_CUDA, std::string("mlp: GEMM shared memory: ") + cudaGetErrorString(e));
+  dim3 grid(1, M / clsph_nn::kGtRows, K / k_split);
+  kernel<<<grid, clsph_nn::kGtThreads, clsph_nn::kGtSmem, s>>>(A, lda, B, ldb, K, k_split, epi, err);
+  return 0;
+}
+
+// the training GEMMs' wait timeouts since the last check
+int check_train_waits(clsph_mlp* m) {
+  uint32_t e = 0;
+  CUDA_TRY(cudaStreamSynchronize(m->stream));
+  CUDA_TRY(cudaMemcpy(&e, m->err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e & kTrainWaitBit) {
+    const uint32_t keep = e & ~kTrainWaitBit;
+    CUDA_TRY(cudaMemcpy(m->err, &keep, sizeof(keep), cudaMemcpyHostToDevice));
+    return fail(CLSPH_ERR_CUDA, "mlp: a tensor-core wait of a training GEMM timed out");
+  }
+  return 0;
+}
+
 template <class T>
 int alloc(T** p, size_t count) {
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
@@ -452,13 +487,14 @@ int pass(clsph_mlp* m, uint32_t rows, float* loss_slot, bool backward) {
   const float* p = m->blob;
   int rc;
   if (backward) CUDA_TRY(cudaMemsetAsync(m->grad, 0, sizeof(float) * kParams, s));
+  uint32_t* err = m->err;
   // Z1 = X W1 + b1, H1 = GELU(Z1)
-  if ((rc = gemm<2, 2, true, false>(s, m->xb, kIn, m->w1b, kHid, rows, kHid, kIn, kIn,
-                                    EpiHidden{p + clsph_nn::kOffB1, m->z1, m->h1, kHid})))
+  if ((rc = gemm_tc<kHid, true, false>(s, err, m->xb, kIn, m->w1b, kHid, rows, kHid, kIn, kIn,
+                                       EpiHidden{p + clsph_nn::kOffB1, m->z1, m->h1, kHid})))
     return rc;
   // Z2 = H1 W2 + b2, H2 = GELU(Z2)
-  if ((rc = gemm<2, 2, true, false>(s, m->h1, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
-                                    EpiHidden{p + clsph_nn::kOffB2, m->z2, m->h2, kHid})))
+  if ((rc = gemm_tc<kHid, true, false>(s, err, m->h1, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
+                                       EpiHidden{p + clsph_nn::kOffB2, m->z2, m->h2, kHid})))
     return rc;
   // Y = H2 W3 + b3, loss, dZ2, dW3, db3
   clsph_nn::k_head<<<rows / 256, kHid, 0, s>>>(m->h2, m->z2, p + clsph_nn::kOffW3, p + clsph_nn::kOffB3, m->yb,
@@ -468,19 +504,20 @@ int pass(clsph_mlp* m, uint32_t rows, float* loss_slot, bool backward) {
   const int splits = rows / kSplitK;
   const size_t split_stride = (size_t)kHid * kHid;
   // dW2 = H1^T dZ2 (split over rows), db2 = column sums of dZ2
-  if ((rc = gemm<2, 2, false, false>(s, m->h1, kHid, m->dz2, kHid, kHid, kHid, rows, kSplitK,
-                                     EpiPartial{m->ws, kHid, split_stride})))
+  if ((rc = gemm_tc<kHid, false, false>(s, err, m->h1, kHid, m->dz2, kHid, kHid, kHid, rows, kSplitK,
+                                        EpiPartial{m->ws, kHid, split_stride})))
     return rc;
   clsph_nn::k_reduce_splits<<<(kHid * kHid + 255) / 256, 256, 0, s>>>(m->ws, splits, (size_t)kHid * kHid,
                                                                       m->grad + clsph_nn::kOffW2);
   clsph_nn::k_colsum<<<rows / 256, kHid, 0, s>>>(m->dz2, rows, kHid, 256, m->grad + clsph_nn::kOffB2);
   // dZ1 = (dZ2 W2^T) * GELU'(Z1)
-  if ((rc = gemm<2, 2, true, true>(s, m->dz2, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
-                                   EpiGeluGrad{m->z1, m->dz1, kHid})))
+  if ((rc = gemm_tc<kHid, true, true>(s, err, m->dz2, kHid, m->w2b, kHid, rows, kHid, kHid, kHid,
+                                      EpiGeluGrad{m->z1, m->dz1, kHid})))
     return rc;
-  // dW1 = X^T dZ1, db1
-  if ((rc = gemm<1, 4, false, false>(s, m->xb, kIn, m->dz1, kHid, kIn, kHid, rows, kSplitK,
-                                     EpiPartial{m->ws, kHid, (size_t)kIn * kHid})))
+  // dW1 = X^T dZ1 as its transpose dZ1^T X (M = 256 hidden rows, N = 32
+  // inputs, stored transposed), db1
+  if ((rc = gemm_tc<kIn, false, false>(s, err, m->dz1, kHid, m->xb, kIn, kHid, kIn, rows, kSplitK,
+                                       clsph_nn::EpiPartialT{m->ws, kHid, (size_t)kIn * kHid})))
     return rc;
   clsph_nn::k_reduce_splits<<<(kIn * kHid + 255) / 256, 256, 0, s>>>(m->ws, splits, (size_t)kIn * kHid,
                                                                     m->grad + clsph_nn::kOffW1);
@@ -892,6 +929,7 @@ int clsph_mlp_gradients(clsph_mlp* m, const float* x_raw, const float* y_raw, ui
   if (grads_host)
     CUDA_TRY(cudaMemcpyAsync(grads_host, m->grad, sizeof(float) * kParams, cudaMemcpyDeviceToHost, m->stream));
   CUDA_TRY(cudaStreamSynchronize(m->stream));
+  if ((rc = check_train_waits(m))) return rc;
   if (loss) *loss = l / rows;
   return CLSPH_OK;
 }
@@ -915,6 +953,7 @@ int clsph_mlp_loss(clsph_mlp* m, const float* x_raw, const float* y_raw, uint64_
   }
   float l = 0.f;
   CUDA_TRY(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
+  if ((rc = check_train_waits(m))) return rc;
   *loss = l / (float)(blocks * rows);
   return CLSPH_OK;
 }
@@ -995,7 +1034,7 @@ int clsph_mlp_train(clsph_mlp* m, const float* x_raw, const float* y_raw, uint64
     }
   }
   if (logged) *logged = nlog;
-  return CLSPH_OK;
+  return check_train_waits(m);
 }
 
 // ---- collector

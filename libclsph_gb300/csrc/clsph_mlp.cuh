@@ -488,6 +488,19 @@ struct EpiPartial {
   }
 };
 
+// split-K partial sums of a transposed product: the GEMM computes C^T, so
+// element (row, col) of it is C's (col, row), ws[blockIdx.z][col][ld]
+struct EpiPartialT {
+  float* ws;
+  int ld;
+  size_t split_stride;
+  __device__ void operator()(int row, int col, float v0, float v1) const {
+    float* w = ws + blockIdx.z * split_stride + row;
+    w[(size_t)col * ld] = v0;
+    w[(size_t)(col + 1) * ld] = v1;
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Training: elementwise and reduction kernels
 

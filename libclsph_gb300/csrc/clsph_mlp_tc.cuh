@@ -386,4 +386,184 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Training GEMM on the tensor cores: C[M x N] = A[M x K] B[K x N] with BF16
+// operands and FP32 accumulation in tensor memory; one CTA of 4 warps per
+// 128-row tile of C and all N <= 256 columns, split-K over blockIdx.z, and
+// the epilogue functors of k_gemm on every (row, even column) pair.
+// A_K: A is stored with K contiguous (row m at A + m lda), else with M
+// contiguous (A^T in memory: row k at A + k lda). B_K: B is stored with K
+// contiguous per column n (B + n ldb), else with N contiguous (row k at
+// B + k ldb). Operands are staged 32 K at a time, double-buffered, into the
+// canonical no-swizzle K-major core-matrix layout of the inference kernel
+// (element (r, k) at (r / 8) * 512 + (k / 8) * 128 + (r % 8) * 16 +
+// (k % 8) * 2): 16-byte vectors when K is contiguous in memory, else 8
+// two-byte stores per 16-byte vector (the transpose). Thread 0 issues two
+// M128 x N x K16 MMAs per chunk and commits them to the chunk buffer's
+// mbarrier; a buffer is restaged once the MMAs that read it have completed.
+// Every wait is bounded: one that runs out sets *err, the CTA stops issuing,
+// waits (bounded) for its last commit and frees tensor memory.
+constexpr int kGtRows = 128;
+constexpr int kGtBK = 32;
+constexpr int kGtThreads = 128;
+constexpr uint32_t kGtSmem = 100 * 1024;  // also keeps two CTAs per SM (512 TMEM columns)
+
+template <int BN>
+struct GemmTcLayout {
+  static_assert(BN % 16 == 0 && BN >= 32 && BN <= 256, "N of an M128 MMA");
+  static constexpr uint32_t kA = kGtRows * kGtBK * 2;
+  static constexpr uint32_t kB = BN * kGtBK * 2;
+  static constexpr uint32_t kStage = kA + kB;
+  static constexpr uint32_t kBar = 2 * kStage;  // two mbarriers
+  static constexpr uint32_t kSlot = kBar + 16;  // tensor-memory address
+  static constexpr uint32_t kBytes = kSlot + 16;
+  static constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static constexpr uint32_t kIdesc = tc_idesc(kGtRows, BN);
+  static_assert(kBytes <= kGtSmem, "shared memory of the tensor-core GEMM");
+};
+
+__device__ __forceinline__ void st_shared_u16(uint32_t addr, uint16_t v) {
+  asm volatile("st.shared.u16 [%0], %1;\n" ::"r"(addr), "h"(v) : "memory");
+}
+
+// 32 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+      "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// `rows` x 32 K of an operand into the canonical layout at `dst`: K-major in
+// memory (row r at src + r ld, K contiguous) or MN-major (K row k at
+// src + k ld, the rows contiguous)
+template <bool KMAJOR>
+__device__ __forceinline__ void gt_stage(uint32_t dst, const bf16* __restrict__ src, int ld, int rows) {
+  if constexpr (KMAJOR) {
+    for (int c = threadIdx.x; c < rows * 4; c += kGtThreads) {
+      const int r = c >> 2, q = c & 3;
+      const uint4 v = *reinterpret_cast<const uint4*>(src + (size_t)r * ld + q * 8);
+      st_shared_v4(dst + (r >> 3) * 512 + q * 128 + (r & 7) * 16, v);
+    }
+  } else {
+    const int vecs = rows / 8;
+    for (int c = threadIdx.x; c < kGtBK * vecs; c += kGtThreads) {
+      const int k = c / vecs, mq = c % vecs;
+      const uint4 v = *reinterpret_cast<const uint4*>(src + (size_t)k * ld + mq * 8);
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+      const uint32_t base = dst + mq * 512 + (k >> 3) * 128 + (k & 7) * 2;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        st_shared_u16(base + e * 16, (uint16_t)(e & 1 ? w[e >> 1] >> 16 : w[e >> 1] & 0xFFFFu));
+    }
+  }
+}
+
+template <int BN, bool A_K, bool B_K, class Epi>
+__global__ void __launch_bounds__(kGtThreads, 1)
+    k_gemm_tc(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B, int ldb, int K, int k_split,
+              Epi epi, uint32_t* __restrict__ err) {
+  using L = GemmTcLayout<BN>;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const uint32_t sb = smem_addr(smem);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kGtRows;
+  const int k_begin = blockIdx.z * k_split;
+  const int k_end = min(K, k_begin + k_split);
+  const int chunks = (k_end - k_begin) / kGtBK;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(sb + L::kSlot),
+                 "r"(L::kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(sb + L::kBar) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(sb + L::kBar + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  auto stage = [&](int buf, int k0) {
+    const uint32_t a = sb + buf * L::kStage, b = a + L::kA;
+    if constexpr (A_K) gt_stage<true>(a, A + (size_t)m0 * lda + k0, lda, kGtRows);
+    else gt_stage<false>(a, A + (size_t)k0 * lda + m0, lda, kGtRows);
+    if constexpr (B_K) gt_stage<true>(b, B + k0, ldb, BN);
+    else gt_stage<false>(b, B + (size_t)k0 * ldb, ldb, BN);
+    fence_async_smem();
+  };
+  if (chunks > 0) stage(0, k_begin);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + L::kSlot);
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  int issued = 0;  // chunks whose MMAs have been issued
+  for (int c = 0; c < chunks && ok; ++c) {
+    const int buf = c & 1;
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a = sb + buf * L::kStage, b = a + L::kA;
+#pragma unroll
+      for (int ks = 0; ks < kGtBK / 16; ++ks)
+        tc_mma(tmem, tc_desc(a + ks * 256, 128, 512), tc_desc(b + ks * 256, 128, 512), L::kIdesc,
+               (c > 0 || ks > 0) ? 1u : 0u);
+      tc_commit(sb + L::kBar + 8 * buf);
+    }
+    issued = c + 1;
+    if (c + 1 < chunks) {
+      const int nb = buf ^ 1;
+      if (c >= 1) {  // the MMAs of chunk c - 1 read buffer nb
+        const bool got = tc_wait(sb + L::kBar + 8 * nb, ph[nb], kTcWaitLimit);
+        if (got) ph[nb] ^= 1u;
+        ok = __syncthreads_and(got);
+        if (!ok) break;
+      }
+      stage(nb, k_begin + (c + 1) * kGtBK);
+      tc_fence_before();
+      __syncthreads();
+    }
+  }
+  // the last commit covers every MMA issued before it
+  bool done = issued == 0;
+  if (issued > 0) {
+    const int lb = (issued - 1) & 1;
+    // a barrier whose earlier commit was not waited for completes twice
+    // before the last phase: wait for that one first
+    if (issued >= 2 && ok) {
+      const int ob = lb ^ 1;
+      if (tc_wait(sb + L::kBar + 8 * ob, ph[ob], kTcWaitLimit)) ph[ob] ^= 1u;
+    }
+    done = tc_wait(sb + L::kBar + 8 * lb, ph[lb], kTcWaitLimit);
+  }
+  if (!__syncthreads_and(done && ok) && tid == 0) atomicOr(err, 1u);
+  tc_fence_after();
+  if (done && ok) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tc_ld32(t_row + c0, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) epi(row, c0 + 2 * j, v[2 * j], v[2 * j + 1]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(L::kCols)
+                 : "memory");
+  }
+}
+
 }  // namespace clsph_nn

@@ -24,6 +24,7 @@ SEARCH_MODES = (SEARCH_WINDOW, SEARCH_CELL_WARPS, SEARCH_PARTICLE_WARPS)
 WARN_GRID_OVERFLOW, WARN_COLLISION_CAP, WARN_NONFINITE = 1, 2, 4
 # bounds of the device waits (clsph_gpu_set_wait_limits)
 DEFAULT_LOOKBACK_SPINS, DEFAULT_MLP_WAIT_POLLS, NO_TILE = 1 << 20, 1 << 24, 0xFFFFFFFF
+DEFAULT_BARRIER_SPINS, NO_BLOCK = 1 << 22, 0xFFFFFFFF
 
 _vp = ctypes.c_void_p
 _u32 = ctypes.c_uint32
@@ -59,6 +60,10 @@ SIGNATURES = [
     ("clsph_gpu_set_launch_shape", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u32]),
     ("clsph_gpu_set_neighbour_search", ctypes.c_int, [_vp, ctypes.c_int]),
     ("clsph_gpu_set_wait_limits", ctypes.c_int, [_vp, _u32, _u32, _u32]),
+    ("clsph_gpu_set_persistent", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("clsph_gpu_set_barrier_limits", ctypes.c_int, [_vp, _u32, _u32]),
+    ("clsph_gpu_read_face_lists", ctypes.c_int,
+     [_vp, _u32, _vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64, _vp]),
     ("clsph_gpu_last_error", ctypes.c_char_p, []),
 ]
 
@@ -288,6 +293,33 @@ class GpuSolver:
         _check("clsph_gpu_set_wait_limits",
                self.lib.clsph_gpu_set_wait_limits(self.h, radix_lookback_spins, mlp_wait_polls,
                                                   radix_withheld_tile))
+
+    def set_persistent(self, on: bool) -> None:
+        """Whole substeps as one persistent cooperative launch (see clsph_gpu.h)."""
+        _check("clsph_gpu_set_persistent", self.lib.clsph_gpu_set_persistent(self.h, 1 if on else 0))
+
+    def set_barrier_limits(self, barrier_spins: int = DEFAULT_BARRIER_SPINS,
+                           withheld_block: int = NO_BLOCK) -> None:
+        _check("clsph_gpu_set_barrier_limits",
+               self.lib.clsph_gpu_set_barrier_limits(self.h, barrier_spins, withheld_block))
+
+    def face_lists(self, scene: int = 0):
+        """(plan dict, CSR starts, face lists) of the scene's per-cell
+        triangle lists as built on the device; (None, None, None) without."""
+        sizes = np.zeros(2, dtype=np.uint32)
+        plan = np.zeros(10, dtype=np.float32)
+        _check("clsph_gpu_read_face_lists",
+               self.lib.clsph_gpu_read_face_lists(self.h, scene, _a(plan), None, 0, None, 0, _a(sizes)))
+        if sizes[0] == 0:
+            return None, None, None
+        start = np.zeros(int(sizes[0]), dtype=np.uint32)
+        faces = np.zeros(max(int(sizes[1]), 1), dtype=np.uint32)
+        _check("clsph_gpu_read_face_lists",
+               self.lib.clsph_gpu_read_face_lists(self.h, scene, None, _a(start), len(start), _a(faces),
+                                                  len(faces), _a(sizes)))
+        info = {"glo": plan[0:3].copy(), "cell": plan[3], "pad": plan[4], "tol": plan[5],
+                "dims": plan[6:9].astype(np.int64), "reach": plan[9]}
+        return info, start, faces[: int(sizes[1])]
 
     def counters(self) -> dict:
         c = np.zeros(3, dtype=np.uint64)

@@ -115,3 +115,69 @@ def test_launch_shapes_do_not_change_results(gpu_lib, shape):
             g.step(4)
             outs.append(g.download())
     assert np.array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
+
+
+def _run_mode(scenes, steps, persistent, density_block=None):
+    with GpuSolver.batched([s.params for s in scenes], [s.terms for s in scenes],
+                           [s.n for s in scenes], [s.mesh for s in scenes]) as b:
+        if density_block is not None:
+            b.set_launch_shape(density_block, 128, 8)
+        b.set_persistent(persistent)
+        b.upload(np.concatenate([s.particles for s in scenes]))
+        b.step(steps)
+        flags = b.sync()
+        out = b.download()
+        keys, perm = b.keys()
+        ids = b.ids()
+    return flags, out, keys, perm, ids
+
+
+@pytest.mark.parametrize("steps", [1, 6, 67])
+def test_persistent_substeps_equal_launched(gpu_lib, steps):
+    """The persistent cooperative launch (every phase of the substep in one
+    kernel, grid barriers between phases) against launched kernels, on
+    scenes of uneven sizes: the state, the sort and the particle ids bit for
+    bit (67 substeps span two launches of at most 64)."""
+    scenes = scene_set(7, seed=70)
+    want = _run_mode(scenes, steps, False, density_block=256)  # the same 8-warp density tiles
+    got = _run_mode(scenes, steps, True)
+    assert got[0] == want[0] == 0
+    assert np.array_equal(got[1].view(np.uint8), want[1].view(np.uint8))
+    for a, b in zip(got[2:], want[2:]):
+        assert np.array_equal(a, b)
+
+
+def test_persistent_dam_break_1m_equals_launched(gpu_lib):
+    sc = W.dam_break_1m()
+    want = _run_mode([sc], 4, False, density_block=256)
+    got = _run_mode([sc], 4, True)
+    assert got[0] == want[0] == 0
+    assert np.array_equal(got[1].view(np.uint8), want[1].view(np.uint8))
+    assert np.array_equal(got[4], want[4])
+
+
+def test_persistent_barrier_wait_runs_out_and_reports(gpu_lib):
+    """Block 0 leaves at the first grid barrier (a block that never arrives,
+    through the barrier test hook), so every other block's bounded wait runs
+    out; clsph_gpu_sync reports it and resets the barrier, and the same
+    handle then steps exactly like a fresh one."""
+    from libclsph_gb300.gpu import ClsphError
+
+    scenes = scene_set(3, seed=75)
+    parts = np.concatenate([s.particles for s in scenes])
+    want = _run_mode(scenes, 2, True)
+    with GpuSolver.batched([s.params for s in scenes], [s.terms for s in scenes],
+                           [s.n for s in scenes], [s.mesh for s in scenes]) as b:
+        b.set_persistent(True)
+        b.set_barrier_limits(barrier_spins=256, withheld_block=0)
+        b.upload(parts)
+        b.step(1)
+        with pytest.raises(ClsphError) as err:
+            b.sync()
+        assert err.value.code == 512 and "grid barrier" in str(err.value)
+        b.set_barrier_limits()
+        b.upload(parts)
+        b.step(2)
+        assert b.sync() == 0
+        out = b.download()
+    assert np.array_equal(out.view(np.uint8), want[1].view(np.uint8))
