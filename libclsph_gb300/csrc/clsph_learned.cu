@@ -379,18 +379,6 @@ namespace {
 using clsph_nn::EpiGeluGrad;
 using clsph_nn::EpiHidden;
 using clsph_nn::EpiPartial;
-using clsph_nn::GemmSmem;
-
-template <int WM, int WN, bool A_K, bool B_K, class Epi>
-int gemm(cudaStream_t s, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int k_split,
-         Epi epi) {
-  using S = GemmSmem<WM, WN, A_K, B_K>;
-  if (M % S::BM || N % S::BN || K % k_split || k_split % clsph_nn::kGemmBK || lda % 8 || ldb % 8)
-    return fail(CLSPH_ERR_ARGUMENT, "mlp: GEMM shape not tileable");
-  dim3 grid(N / S::BN, M / S::BM, K / k_split);
-  clsph_nn::k_gemm<WM, WN, A_K, B_K, Epi><<<grid, 128, S::BYTES, s>>>(A, lda, B, ldb, M, N, K, k_split, epi);
-  return 0;
-}
 
 // Training GEMMs on the tensor cores (clsph_nn::k_gemm_tc); timeouts of its
 // bounded waits set bit kTrainWaitBit of the network's error word.

@@ -8,10 +8,9 @@
 //                 layer 2, layer-2 outputs are consumed 64 columns at a time
 //                 by layer 3, so nothing but the 64-byte feature row is read
 //                 and one float4 written per particle.
-//   k_gemm        tiled GEMM for training, C = A * B with either operand
-//                 stored contraction-major or not (ldmatrix / ldmatrix.trans),
-//                 cp.async double buffering, split-K over blockIdx.z and an
-//                 epilogue functor (bias + GELU, GELU', split partials).
+//   Epi*          epilogue functors of the training GEMMs (bias + GELU,
+//                 GELU', split partials), which run on the tcgen05 tensor
+//                 cores (k_gemm_tc, clsph_mlp_tc.cuh).
 //   k_head_*, k_colsum, k_reduce_splits, k_adam, k_gather_batch: the
 //                 elementwise and reduction parts of one training iteration.
 //
@@ -55,12 +54,6 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(addr));
-}
-
 __device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], uint32_t addr) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];\n"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
@@ -83,14 +76,6 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* gptr) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr), "l"(gptr));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
 
 // Standardised inputs are clamped to +-kInputClamp (training and inference
 // alike): states outside the training distribution cannot drive the network
@@ -337,119 +322,8 @@ __global__ void __launch_bounds__(kInferWarps * 32, 1)
 // Tiled GEMM for training: C[M][N] = sum_k A[m][k] * B[k][n].
 // A_K: A stored [M][K] (lda = row stride), else stored [K][M].
 // B_K: B stored [N][K], else stored [K][N].
-// Four warps in a WM x WN arrangement, 32 x 32 per warp; BK = 32.
-// Requires M % (32 WM) == 0, N % (32 WN) == 0, K-split lengths % 32 == 0 and
-// 16-byte aligned rows (checked by the host).
-
-constexpr int kGemmBK = 32;
-
-template <int WM, int WN, bool A_K, bool B_K>
-struct GemmSmem {
-  static constexpr int BM = WM * 32, BN = WN * 32;
-  static constexpr int A_ROWS = A_K ? BM : kGemmBK;
-  static constexpr int A_STRIDE = (A_K ? kGemmBK : BM) + 8;
-  static constexpr int B_ROWS = B_K ? BN : kGemmBK;
-  static constexpr int B_STRIDE = (B_K ? kGemmBK : BN) + 8;
-  static constexpr int A_ELEMS = A_ROWS * A_STRIDE;
-  static constexpr int B_ELEMS = B_ROWS * B_STRIDE;
-  static constexpr size_t BYTES = 2 * sizeof(bf16) * (A_ELEMS + B_ELEMS);
-};
-
-template <int WM, int WN, bool A_K, bool B_K, class Epi>
-__global__ void __launch_bounds__(128)
-    k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B, int ldb, int M, int N,
-           int K, int k_split, Epi epi) {
-  using S = GemmSmem<WM, WN, A_K, B_K>;
-  constexpr int BM = S::BM, BN = S::BN;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  bf16* sA = reinterpret_cast<bf16*>(smem_raw);
-  bf16* sB = sA + 2 * S::A_ELEMS;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int k_begin = blockIdx.z * k_split;
-  const int k_end = min(K, k_begin + k_split);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wm = warp % WM, wn = warp / WM;
-  const int g = lane >> 2, tig = lane & 3, lr = lane & 7, lj = lane >> 3;
-
-  auto load_stage = [&](int stage, int k0) {
-    bf16* a = sA + stage * S::A_ELEMS;
-    bf16* b = sB + stage * S::B_ELEMS;
-    if constexpr (A_K) {  // BM rows of 32 k: 4 chunks per row
-      for (int c = threadIdx.x; c < BM * 4; c += 128) {
-        const int r = c >> 2, q = c & 3;
-        cp_async16(smem_addr(a + r * S::A_STRIDE + q * 8), A + (size_t)(m0 + r) * lda + k0 + q * 8);
-      }
-    } else {  // 32 k rows of BM m
-      for (int c = threadIdx.x; c < kGemmBK * (BM / 8); c += 128) {
-        const int r = c / (BM / 8), q = c % (BM / 8);
-        cp_async16(smem_addr(a + r * S::A_STRIDE + q * 8), A + (size_t)(k0 + r) * lda + m0 + q * 8);
-      }
-    }
-    if constexpr (B_K) {
-      for (int c = threadIdx.x; c < BN * 4; c += 128) {
-        const int r = c >> 2, q = c & 3;
-        cp_async16(smem_addr(b + r * S::B_STRIDE + q * 8), B + (size_t)(n0 + r) * ldb + k0 + q * 8);
-      }
-    } else {
-      for (int c = threadIdx.x; c < kGemmBK * (BN / 8); c += 128) {
-        const int r = c / (BN / 8), q = c % (BN / 8);
-        cp_async16(smem_addr(b + r * S::B_STRIDE + q * 8), B + (size_t)(k0 + r) * ldb + n0 + q * 8);
-      }
-    }
-    cp_async_commit();
-  };
-
-  float acc[2][4][4] = {};
-  const int steps = (k_end - k_begin) / kGemmBK;
-  if (steps > 0) load_stage(0, k_begin);
-  for (int s = 0; s < steps; ++s) {
-    if (s + 1 < steps) {
-      load_stage((s + 1) & 1, k_begin + (s + 1) * kGemmBK);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    __syncthreads();
-    const bf16* a = sA + (s & 1) * S::A_ELEMS;
-    const bf16* b = sB + (s & 1) * S::B_ELEMS;
-#pragma unroll
-    for (int kk = 0; kk < kGemmBK; kk += 16) {
-      uint32_t af[2][4];
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const int r0 = wm * 32 + mt * 16;
-        if constexpr (A_K)
-          ldsm_x4(af[mt], smem_addr(a + (r0 + lr + (lj & 1) * 8) * S::A_STRIDE + kk + (lj >> 1) * 8));
-        else
-          ldsm_x4_t(af[mt], smem_addr(a + (kk + lr + (lj >> 1) * 8) * S::A_STRIDE + r0 + (lj & 1) * 8));
-      }
-#pragma unroll
-      for (int np = 0; np < 2; ++np) {
-        const int c0 = wn * 32 + np * 16;
-        uint32_t bf[4];
-        if constexpr (B_K)
-          ldsm_x4(bf, smem_addr(b + (c0 + lr + (lj >> 1) * 8) * S::B_STRIDE + kk + (lj & 1) * 8));
-        else
-          ldsm_x4_t(bf, smem_addr(b + (kk + lr + (lj & 1) * 8) * S::B_STRIDE + c0 + (lj >> 1) * 8));
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-          mma16816(acc[mt][2 * np], af[mt], bf[0], bf[1]);
-          mma16816(acc[mt][2 * np + 1], af[mt], bf[2], bf[3]);
-        }
-      }
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const int row = m0 + wm * 32 + mt * 16 + g;
-      const int col = n0 + wn * 32 + nt * 8 + tig * 2;
-      epi(row, col, acc[mt][nt][0], acc[mt][nt][1]);
-      epi(row + 8, col, acc[mt][nt][2], acc[mt][nt][3]);
-    }
-}
+// Epilogue functors of the training GEMM (k_gemm_tc in clsph_mlp_tc.cuh),
+// called on every (row, even column) pair of the product.
 
 // z = acc + bias; Z (fp32) and H = GELU(z) (bf16), both [M][ld]
 struct EpiHidden {
