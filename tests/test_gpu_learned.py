@@ -375,3 +375,35 @@ def test_collector_on_learned_rollout(gpu_lib):
     assert count == steps * ((sc.n + stride - 1) // stride)
     assert np.isfinite(x).all() and np.isfinite(y).all()
     m.close()
+
+
+def test_committed_weights_behaviour_on_dam_break_32k(gpu_lib):
+    """The committed network (libclsph_gb300/weights/stepper_4dt.npz) on the
+    32,768-particle dam break over 400 plain substeps' time (100 learned
+    steps), against the plain solver, with and without the 1 % density check,
+    and against a network whose every output is 0 (the bare 4 dt step):
+    finite states, and density deviations within bounds, so a change of the
+    weights or of the learned step that worsens them shows."""
+    from libclsph_gb300.stepper_eval import evaluate
+
+    path = Lm.default_weights_path()
+    if not path.exists():
+        pytest.skip("no committed weights")
+    sc = W.dam_break_32k()
+    net = Lm.Mlp.load(path)
+    zero = Lm.Mlp(blob=identity_blob())
+    try:
+        checked = evaluate(sc, net, plain_substeps=400, checkpoints=4, threshold=0.01)
+        free = evaluate(sc, net, plain_substeps=400, checkpoints=4, check=False)
+        bare = evaluate(sc, zero, plain_substeps=400, checkpoints=4, check=False)
+    finally:
+        net.close()
+        zero.close()
+    report = {k: (r["density_dev"], r["density_dev_max"], r["fallback_fraction"], r["pos_rms_h_final"])
+              for k, r in (("checked", checked), ("free", free), ("zero", bare))}
+    print("committed weights on the 32k dam break (density_dev, max, fallback, pos_rms_h):", report)
+    for r in (checked, free, bare):
+        assert np.isfinite(r["density_dev"]) and np.isfinite(r["pos_rms_h_final"])
+    assert checked["accepted_steps"] + checked["rejected_steps"] > 0
+    assert checked["density_dev"] <= 0.05
+    assert free["density_dev"] <= bare["density_dev"] + 0.03
