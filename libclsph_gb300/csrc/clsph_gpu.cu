@@ -334,44 +334,54 @@ int plan_face_grid(const clsph_parameters& p, const float* vx, uint32_t nv, cons
 // sm.cell_start / sm.cell_faces.
 int build_face_lists(clsph_gpu* h, SceneMesh& sm, uint32_t faces, const FaceGridPlan& g) {
   const uint32_t cells = g.cells;
-  const uint32_t fblocks = grid_blocks(faces, h->sm_count * 8);
-  uint32_t *count = nullptr, *sums = nullptr, *fill = nullptr;
+  if (faces > kScanBlock * kScanThreads) return fail(CLSPH_ERR_TOO_LARGE, "face lists: more than 2^22 faces");
+  uint32_t *count = nullptr, *csums = nullptr, *fill = nullptr, *face_n = nullptr, *face_start = nullptr,
+           *fsums = nullptr;
   unsigned long long* entries = nullptr;
   int rc = 0;
   auto done = [&](int code) {
-    cudaFree(count);
-    cudaFree(sums);
-    cudaFree(fill);
-    cudaFree(entries);
+    void* bufs[] = {count, csums, fill, face_n, face_start, fsums, entries};
+    for (void* b : bufs) cudaFree(b);
     return code;
   };
-  const uint32_t sblocks = (cells + kScanBlock - 1) / kScanBlock;
-  if ((rc = dev_alloc(&count, cells)) || (rc = dev_alloc(&sums, sblocks + 1)) || (rc = dev_alloc(&fill, cells)) ||
-      (rc = dev_alloc(&entries, 1)) || (rc = dev_alloc(&sm.cell_start, (size_t)cells + 1)))
+  const uint32_t cblocks = (cells + kScanBlock - 1) / kScanBlock;
+  const uint32_t fblocks_scan = (faces + kScanBlock - 1) / kScanBlock;
+  if ((rc = dev_alloc(&count, cells)) || (rc = dev_alloc(&csums, cblocks + 1)) || (rc = dev_alloc(&fill, cells)) ||
+      (rc = dev_alloc(&face_n, faces)) || (rc = dev_alloc(&face_start, (size_t)faces + 1)) ||
+      (rc = dev_alloc(&fsums, fblocks_scan + 1)) || (rc = dev_alloc(&entries, 1)) ||
+      (rc = dev_alloc(&sm.cell_start, (size_t)cells + 1)))
     return done(rc);
   cudaStream_t s = h->stream;
   cudaError_t e = cudaMemsetAsync(entries, 0, sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(uint32_t) * cells, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(fill, 0, sizeof(uint32_t) * cells, s);
   if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
-  k_face_entries<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, entries);
+  k_face_entries<<<grid_blocks(faces, h->sm_count * 8), kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, face_n,
+                                                                         entries);
   unsigned long long total = 0;
   e = cudaMemcpyAsync(&total, entries, sizeof(total), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
   if (total > 0x7FFFFFFFull) return done(fail(CLSPH_ERR_TOO_LARGE, "face lists too large"));
+  const uint32_t n_entries = (uint32_t)total;
   if ((rc = dev_alloc(&sm.cell_faces, total ? total : 1))) return done(rc);
-  k_face_count<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, count);
-  k_scan_sums<<<sblocks, kScanThreads, 0, s>>>(count, cells, sums);
-  k_scan_top<<<1, kScanThreads, 0, s>>>(sums, sblocks, sm.cell_start + cells);
-  k_scan_apply<<<sblocks, kScanThreads, 0, s>>>(count, cells, sums, sm.cell_start);
-  k_face_fill<<<fblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, sm.cell_start, fill, sm.cell_faces);
+  // entry starts of the faces, then the cells' counts and CSR starts
+  k_scan_sums<<<fblocks_scan, kScanThreads, 0, s>>>(face_n, faces, fsums);
+  k_scan_top<<<1, kScanThreads, 0, s>>>(fsums, fblocks_scan, face_start + faces);
+  k_scan_apply<<<fblocks_scan, kScanThreads, 0, s>>>(face_n, faces, fsums, face_start);
+  const uint32_t eblocks = grid_blocks(n_entries, h->sm_count * 16);
+  k_face_count<<<eblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, face_start, n_entries, count);
+  k_scan_sums<<<cblocks, kScanThreads, 0, s>>>(count, cells, csums);
+  k_scan_top<<<1, kScanThreads, 0, s>>>(csums, cblocks, sm.cell_start + cells);
+  k_scan_apply<<<cblocks, kScanThreads, 0, s>>>(count, cells, csums, sm.cell_start);
+  k_face_fill<<<eblocks, kBlock, 0, s>>>(sm.vertices, sm.indices, faces, g, face_start, n_entries, sm.cell_start,
+                                         fill, sm.cell_faces);
   k_face_sort<<<grid_blocks(cells, h->sm_count * 8), kBlock, 0, s>>>(sm.cell_start, cells, sm.cell_faces);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return done(fail(CLSPH_ERR_CUDA, std::string("face lists: ") + cudaGetErrorString(e)));
   sm.plan = g;
-  sm.list_len = (uint32_t)total;
+  sm.list_len = n_entries;
   return done(0);
 }
 

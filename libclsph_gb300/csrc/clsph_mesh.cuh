@@ -7,10 +7,12 @@
 // its bounding box, grown by the list reach plus a tolerance, overlaps, and
 // each list holds its faces in ascending order, so scanning one list is the
 // reference's scan over all faces for any segment that starts in the cell and
-// is no longer than the reach (DevMesh::reach). Four kernels:
-//   k_face_count  one thread per face: its cell range, one atomic per cell
-//   k_scan_*      exclusive scan of the counts into the CSR starts
-//   k_face_fill   one thread per face: an atomic slot in each of its cells
+// is no longer than the reach (DevMesh::reach). The kernels:
+//   k_face_entries  one thread per face: the size of its cell range
+//   k_scan_*      exclusive scans: face entries into entry starts, cell
+//                 counts into the CSR starts
+//   k_face_count  one thread per (face, cell) entry: one atomic per cell
+//   k_face_fill   one thread per entry: an atomic slot in the cell's list
 //   k_face_sort   one thread per cell: its list into ascending face order
 // (the atomic fill leaves each list in arbitrary order; the sort restores the
 // order the reference's loop visits faces in).
@@ -47,42 +49,61 @@ __device__ __forceinline__ void face_cell_range(const float* __restrict__ vx, co
   }
 }
 
-template <class F>
-__device__ __forceinline__ void for_face_cells(const float* __restrict__ vx, const uint32_t* __restrict__ ix,
-                                               uint32_t f, const FaceGridPlan& g, F&& fn) {
-  int c0[3], c1[3];
-  face_cell_range(vx, ix, f, g, c0, c1);
-  for (int z = c0[2]; z <= c1[2]; ++z)
-    for (int y = c0[1]; y <= c1[1]; ++y)
-      for (int x = c0[0]; x <= c1[0]; ++x)
-        fn(((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0] + (uint32_t)x);
-}
-
-// Number of (face, cell) entries, in 64 bits (a check before the 32-bit
-// counts and starts are built).
+// Number of (face, cell) entries of every face (face_n) and their total in
+// 64 bits (a size check before the 32-bit counts and starts are built).
 static __global__ void k_face_entries(const float* __restrict__ vx, const uint32_t* __restrict__ ix,
-                                      uint32_t faces, FaceGridPlan g, unsigned long long* __restrict__ total) {
+                                      uint32_t faces, FaceGridPlan g, uint32_t* __restrict__ face_n,
+                                      unsigned long long* __restrict__ total) {
   unsigned long long mine = 0;
   for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < faces; f += gridDim.x * blockDim.x) {
     int c0[3], c1[3];
     face_cell_range(vx, ix, f, g, c0, c1);
-    mine += (unsigned long long)(c1[0] - c0[0] + 1) * (unsigned long long)(c1[1] - c0[1] + 1) *
-            (unsigned long long)(c1[2] - c0[2] + 1);
+    const unsigned long long e = (unsigned long long)(c1[0] - c0[0] + 1) *
+                                 (unsigned long long)(c1[1] - c0[1] + 1) * (unsigned long long)(c1[2] - c0[2] + 1);
+    face_n[f] = e > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)e;
+    mine += e;
   }
   if (mine) atomicAdd(total, mine);
 }
 
+// The (face, cell) entries spread over all threads, whatever the faces' sizes
+// (a wall of a box meets thousands of cells, a heightfield triangle a few):
+// entry e belongs to the face f with face_start[f] <= e < face_start[f + 1]
+// (binary search) and is cell number e - face_start[f] of f's range, x
+// fastest. Calls fn(f, cell).
+template <class F>
+__device__ __forceinline__ void for_entries(const float* __restrict__ vx, const uint32_t* __restrict__ ix,
+                                            uint32_t faces, const FaceGridPlan& g,
+                                            const uint32_t* __restrict__ face_start, uint32_t entries, F&& fn) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < entries; e += gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = faces;  // last f with face_start[f] <= e
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (face_start[mid] <= e) lo = mid; else hi = mid;
+    }
+    const uint32_t f = lo;
+    int c0[3], c1[3];
+    face_cell_range(vx, ix, f, g, c0, c1);
+    const uint32_t local = e - face_start[f];
+    const uint32_t nx = (uint32_t)(c1[0] - c0[0] + 1), ny = (uint32_t)(c1[1] - c0[1] + 1);
+    const uint32_t x = (uint32_t)c0[0] + local % nx, y = (uint32_t)c0[1] + (local / nx) % ny,
+                   z = (uint32_t)c0[2] + local / (nx * ny);
+    fn(f, (z * (uint32_t)g.dims[1] + y) * (uint32_t)g.dims[0] + x);
+  }
+}
+
 static __global__ void k_face_count(const float* __restrict__ vx, const uint32_t* __restrict__ ix,
-                                    uint32_t faces, FaceGridPlan g, uint32_t* __restrict__ count) {
-  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < faces; f += gridDim.x * blockDim.x)
-    for_face_cells(vx, ix, f, g, [&](uint32_t c) { atomicAdd(&count[c], 1u); });
+                                    uint32_t faces, FaceGridPlan g, const uint32_t* __restrict__ face_start,
+                                    uint32_t entries, uint32_t* __restrict__ count) {
+  for_entries(vx, ix, faces, g, face_start, entries, [&](uint32_t, uint32_t c) { atomicAdd(&count[c], 1u); });
 }
 
 static __global__ void k_face_fill(const float* __restrict__ vx, const uint32_t* __restrict__ ix,
-                                   uint32_t faces, FaceGridPlan g, const uint32_t* __restrict__ start,
+                                   uint32_t faces, FaceGridPlan g, const uint32_t* __restrict__ face_start,
+                                   uint32_t entries, const uint32_t* __restrict__ start,
                                    uint32_t* __restrict__ fill, uint32_t* __restrict__ list) {
-  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < faces; f += gridDim.x * blockDim.x)
-    for_face_cells(vx, ix, f, g, [&](uint32_t c) { list[start[c] + atomicAdd(&fill[c], 1u)] = f; });
+  for_entries(vx, ix, faces, g, face_start, entries,
+              [&](uint32_t f, uint32_t c) { list[start[c] + atomicAdd(&fill[c], 1u)] = f; });
 }
 
 static __global__ void k_face_sort(const uint32_t* __restrict__ start, uint32_t cells, uint32_t* __restrict__ list) {
