@@ -132,17 +132,39 @@ void sph_simulation::simulate(int frame_count) {
                          reinterpret_cast<const clsph_kernel_terms*>(&precomputed_terms), n, &gpu_),
         "clsph_gpu_create");
   check(clsph_gpu_set_collision_cap(gpu_, collision_iteration_cap), "clsph_gpu_set_collision_cap");
-  // The reference hands face_normals.data() with face_count faces to the
-  // kernel (sph_simulation.cpp:296-337): the first face_count normals.
-  if (current_scene.face_count > 0) {
-    if (current_scene.face_normals.size() < 3ull * current_scene.face_count ||
-        current_scene.indices.size() < 3ull * current_scene.face_count)
+  // The reference hands current_scene to the kernels every substep
+  // (sph_simulation.cpp:296-337: face_normals.data() with face_count faces,
+  // the first face_count normals), so a callback may edit the scene in place
+  // and the next substep collides with the edited mesh. The device keeps the
+  // mesh; after a callback the scene is compared with the copy last uploaded
+  // and uploaded again when it differs.
+  unsigned int up_faces = 0;
+  std::vector<float> up_normals, up_vertices;
+  std::vector<unsigned int> up_indices;
+  auto upload_scene = [&]() {
+    const unsigned int faces = current_scene.face_count;
+    if (faces > 0 && (current_scene.face_normals.size() < 3ull * faces ||
+                      current_scene.indices.size() < 3ull * faces))
       throw std::runtime_error("scene arrays are shorter than face_count");
-    check(clsph_gpu_set_mesh(gpu_, current_scene.face_normals.data(), current_scene.vertices.data(),
+    check(clsph_gpu_set_mesh(gpu_, faces ? current_scene.face_normals.data() : nullptr,
+                             faces ? current_scene.vertices.data() : nullptr,
                              (uint32_t)(current_scene.vertices.size() / 3),
-                             current_scene.indices.data(), current_scene.face_count),
+                             faces ? current_scene.indices.data() : nullptr, faces),
           "clsph_gpu_set_mesh");
-  }
+    up_faces = faces;
+    up_normals = current_scene.face_normals;
+    up_vertices = current_scene.vertices;
+    up_indices = current_scene.indices;
+  };
+  if (current_scene.face_count > 0) upload_scene();
+  bool scene_check = false;  // a callback ran since the last comparison
+  auto refresh_scene = [&]() {
+    if (!scene_check) return;
+    scene_check = false;
+    if (current_scene.face_count != up_faces || current_scene.face_normals != up_normals ||
+        current_scene.vertices != up_vertices || current_scene.indices != up_indices)
+      upload_scene();
+  };
 
   std::vector<particle> storage(n);
   particle* particles = storage.data();
@@ -171,6 +193,7 @@ void sph_simulation::simulate(int frame_count) {
   auto callback = [&](const std::function<void(particle*, const simulation_parameters&, bool)>& cb,
                       bool full_frame) {
     if (!cb) return;
+    scene_check = true;
     if (full_frame || transfers == transfer_policy::every_substep) {
       refresh_host();
       cb(particles, parameters, full_frame);
@@ -189,6 +212,7 @@ void sph_simulation::simulate(int frame_count) {
               "clsph_gpu_upload");
         host_dirty = false;
       }
+      refresh_scene();
       check(clsph_gpu_step(gpu_, 1), "clsph_gpu_step");
       device_newer = true;
       callback(post_frame, false);

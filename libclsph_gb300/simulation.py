@@ -83,10 +83,39 @@ class Simulation:
         if frame_count == 0:
             frame_count = int(math.ceil(float(f32(p["simulation_time"]) * f32(p["target_fps"]))))
         n = int(p["particles_count"])
-        mesh = self.current_scene.mesh() if self.current_scene.face_count else None
         particles = self.init_particles()
-        state = {"device_newer": False, "host_dirty": False}
-        with GpuSolver(p, self.precomputed_terms, n, mesh) as gpu:
+        # The reference hands current_scene to the kernels every substep
+        # (sph_simulation.cpp:296-337), so a callback may edit the scene in
+        # place; after a callback the scene is compared with the copy last
+        # uploaded and uploaded again when it differs.
+        state = {"device_newer": False, "host_dirty": False, "scene_check": False, "uploaded": None}
+
+        def scene_copy():
+            sc = self.current_scene
+            return (int(sc.face_count), np.array(sc.face_normals, copy=True), np.array(sc.vertices, copy=True),
+                    np.array(sc.indices, copy=True))
+
+        def upload_scene(gpu):
+            sc = self.current_scene
+            gpu.set_mesh(sc.mesh() if sc.face_count else {"face_normals": np.zeros(0, np.float32),
+                                                           "vertices": np.zeros(0, np.float32),
+                                                           "indices": np.zeros(0, np.uint32)})
+            state["uploaded"] = scene_copy()
+
+        def refresh_scene(gpu):
+            if not state["scene_check"]:
+                return
+            state["scene_check"] = False
+            now, up = scene_copy(), state["uploaded"]
+            if now[0] != up[0] or any(a.shape != b.shape or not np.array_equal(a, b)
+                                      for a, b in zip(now[1:], up[1:])):
+                upload_scene(gpu)
+
+        with GpuSolver(p, self.precomputed_terms, n, None) as gpu:
+            if self.current_scene.face_count:
+                upload_scene(gpu)
+            else:
+                state["uploaded"] = scene_copy()
             gpu.set_collision_cap(self.collision_iteration_cap)
             gpu.upload(particles)
 
@@ -106,6 +135,7 @@ class Simulation:
             def call(cb, full):
                 if cb is None:
                     return
+                state["scene_check"] = True
                 if full or self.transfers == EVERY_SUBSTEP:
                     refresh()
                     cb(particles, self.parameters, full)
@@ -123,6 +153,7 @@ class Simulation:
                     if state["host_dirty"]:
                         gpu.upload(particles)
                         state["host_dirty"] = False
+                    refresh_scene(gpu)
                     gpu.step(1)
                     state["device_newer"] = True
                     call(self.post_frame, False)

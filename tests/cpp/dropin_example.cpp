@@ -1,7 +1,9 @@
 // A libclsph-style driver written against the drop-in headers: load the two
 // property files and a scene, run `frames` frames with pre/post callbacks,
 // write a Houdini frame and the final particle AoS (raw, like last_frame.bin).
-//   dropin_example <fluid.json> <sim.json> <scene.obj> <frames> <out_prefix> [frames_only]
+//   dropin_example <fluid.json> <sim.json> <scene.obj> <frames> <out_prefix> [frames_only|raise_mesh]
+// raise_mesh: the 4th substep's pre_frame callback moves every vertex of the
+// scene up by 0.4995 m, in place (the next substeps collide with the moved mesh).
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -27,12 +29,16 @@ int main(int argc, char** argv) {
   if (!sim.current_scene.load(argv[3])) return 1;
   if (argc > 6 && std::string(argv[6]) == "frames_only")
     sim.transfers = sph_simulation::transfer_policy::frames_only;
+  const bool raise_mesh = argc > 6 && std::string(argv[6]) == "raise_mesh";
+  int substep_calls = 0;
   const std::string prefix = argv[5];
   houdini_file_saver saver(prefix);
   int pre_calls = 0, post_calls = 0;
   sim.pre_frame = [&](particle* p, const simulation_parameters& prm, bool full) {
     ++pre_calls;
     if (full) saver.writeFrameToFile(p, prm);
+    if (!full && ++substep_calls == 4 && raise_mesh)
+      for (size_t v = 1; v < sim.current_scene.vertices.size(); v += 3) sim.current_scene.vertices[v] += 0.4995f;
   };
   sim.post_frame = [&](particle* p, const simulation_parameters& prm, bool full) {
     ++post_calls;

@@ -110,6 +110,49 @@ def test_callback_changes_reach_the_next_substep(gpu_lib, workdir):
     assert np.array_equal(out.view(np.uint8), cur.view(np.uint8))
 
 
+RAISE = np.float32(0.4995)  # moves the cube's top face to just below the lattice's lowest layer
+
+
+def raise_mesh(mesh):
+    out = dict(mesh, vertices=np.array(mesh["vertices"], dtype=np.float32, copy=True))
+    out["vertices"][1::3] += RAISE
+    return out
+
+
+def test_scene_edits_in_callbacks_reach_the_next_substep(gpu_lib, workdir):
+    """The reference hands current_scene to its kernels every substep
+    (sph_simulation.cpp:296-337), so a callback that moves the mesh in place
+    changes the collisions from the next substep on."""
+    sim = make_sim()
+    calls = {"n": 0}
+
+    def move_mesh(p, prm, full):
+        if not full:
+            calls["n"] += 1
+            if calls["n"] == 4:
+                sim.current_scene.vertices[1::3] += RAISE
+
+    sim.pre_frame = move_mesh
+    out = sim.simulate(1)
+    assert calls["n"] == 10
+    # the engine: 3 substeps with the loaded mesh, 7 with the moved one
+    p0 = init_lattice(2744, sim.initial_volume)
+    m0 = make_sim().current_scene.mesh()
+    with GpuSolver(sim.parameters, sim.precomputed_terms, 2744, m0) as g:
+        g.upload(p0)
+        g.step(3)
+        g.set_mesh(raise_mesh(m0))
+        g.step(7)
+        moved = g.download()
+        g.upload(p0)
+        g.set_mesh(m0)
+        g.step(10)
+        still = g.download()
+    assert np.array_equal(out.view(np.uint8), moved.view(np.uint8))
+    # the moved mesh is hit: the edit changes the outcome
+    assert not np.array_equal(moved["position"], still["position"])
+
+
 def test_frames_only_policy_matches_when_callbacks_only_read(gpu_lib, workdir):
     a = make_sim()
     a.pre_frame = lambda p, prm, full: None
@@ -149,3 +192,20 @@ def test_cpp_dropin_example_matches_python(gpu_lib, workdir):
     # one Houdini frame per full frame, named like the reference's
     assert sorted(f.name for f in (workdir / "frames").iterdir()) == [
         "frame0000001.geo", "frame0000002.geo"]
+    # a scene edited in place by a callback reaches the device, as in Python
+    run = subprocess.run([str(exe), "water.json", "sim.json", "cube.obj", "1", "./", "raise_mesh"],
+                         capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr
+    cpp = np.fromfile("final.bin", dtype=PARTICLE)
+    sim = make_sim()
+    calls = {"n": 0}
+
+    def move_mesh(p, prm, full):
+        if not full:
+            calls["n"] += 1
+            if calls["n"] == 4:
+                sim.current_scene.vertices[1::3] += RAISE
+
+    sim.pre_frame = move_mesh
+    py = sim.simulate(1)
+    assert np.array_equal(cpp.view(np.uint8), py.view(np.uint8))
