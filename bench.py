@@ -65,6 +65,35 @@ ALG_BYTES_PER_PARTICLE = {
     "advect": 48 + 48,              # read position, half-step velocity, acceleration; write state
 }
 STEP_ALG_BYTES = 232  # per particle-substep: key read 16 + sort scatter 96 + density 20 + forces/integrate 100
+# FP32 operations of the exact pair arithmetic, one per IEEE add, multiply,
+# divide or square root (the kernels use no FMAs there): a density pair
+# (forces.cl:33-36) and a force pair (forces.cl:67-97), and per particle the
+# Tait pressure with its quotients (sph.cl:36-39) and the acceleration
+# (forces.cl:103-109, sph.cl:53-58)
+FLOP_DENSITY_PAIR = 16
+FLOP_FORCE_PAIR = 65
+FLOP_PER_PARTICLE = 30
+# FP32 peak of a GB300 at its maximum SM clock (2070 MHz): 152 SMs x 128
+# lanes x 2 (an FMA counted as two operations) = 80.5 TFLOP/s
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2070e6 / 1e12
+
+
+def mean_pairs(scene, particles) -> float | None:
+    """Mean number of particles within h of a particle (itself included)
+    in the given state: the pairs the exact arithmetic evaluates."""
+    try:
+        from scipy.spatial import cKDTree
+    except ImportError:
+        return None
+    parts = scene.scenes if isinstance(scene, Batch) else [scene]
+    total, first = 0, 0
+    for s in parts:
+        n = len(s.particles)
+        pos = np.asarray(particles["position"][first:first + n, :3], dtype=np.float64)
+        h = float(s.params["h"])
+        total += int(cKDTree(pos).query_pairs(h, output_type="ndarray").shape[0]) * 2 + n
+        first += n
+    return total / max(first, 1)
 
 def _w():
     return __import__("libclsph_gb300.workloads", fromlist=["x"])
@@ -623,6 +652,17 @@ def main() -> None:
         except Exception:
             traffic = None
     step_achieved = STEP_ALG_BYTES * n * args.steps / device_s / 1e9
+    # FP32 pipe: the exact pair arithmetic over the pairs of the final state
+    pairs = mean_pairs(scene, aos)
+    fp32 = None
+    if pairs is not None:
+        flop = (FLOP_DENSITY_PAIR + FLOP_FORCE_PAIR) * pairs + FLOP_PER_PARTICLE
+        fp32_achieved = flop * value / 1e12
+        fp32 = {"pairs_per_particle": pairs, "flop_per_particle_step": flop, "achieved_tflops": fp32_achieved,
+                "peak_tflops": FP32_PEAK_TFLOPS, "frac": fp32_achieved / FP32_PEAK_TFLOPS,
+                "how": "one FLOP per IEEE add, multiply, divide and square root of the exact density and force "
+                       "pair arithmetic over the neighbour pairs of the final state; peak 152 SMs x 128 lanes x "
+                       "2 x 2070 MHz"}
 
     # ---- learned 4x-dt stepper against the plain solver (the 1M dam break only)
     learned = None
@@ -668,6 +708,7 @@ def main() -> None:
             "mean_launch_ms": dom_mean_s * 1e3,
             "step_alg_GBps": step_achieved,
             "step_frac": step_achieved / peak,
+            "fp32": fp32,
         },
         "kernel_ms_per_step": {k: v[0] / prof_steps for k, v in ktimes.items() if v[1]},
         "long_run": long_run,
