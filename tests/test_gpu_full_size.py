@@ -73,9 +73,11 @@ def test_dam_break_1m_ten_substeps_match_oracle(gpu_lib, oracle, dam_break):
 
 def fp64_report(rho, prs, acc, rho64, prs64, acc64):
     """Relative errors of FP32 fields against FP64 ones: per particle for
-    density and pressure; per particle as |a - a64| / |a64| (median, max) and
-    against the field's largest magnitude for the acceleration, whose sums
-    cancel."""
+    density; for the pressure per particle and against the field's largest
+    magnitude (the Tait pressure K((rho/rho0)^7 - 1) passes through zero at
+    rho0, where its per-particle relative error is unbounded); per particle as
+    |a - a64| / |a64| (median, max) and against the field's largest magnitude
+    for the acceleration, whose sums cancel."""
     def rel(x, y):
         e = np.abs(x.astype(np.float64) - y)
         return e / np.maximum(np.abs(y), 1e-30)
@@ -85,27 +87,39 @@ def fp64_report(rho, prs, acc, rho64, prs64, acc64):
     r_rho, r_p = rel(rho, rho64), rel(prs, prs64)
     return {
         "density": {"max_rel": float(r_rho.max()), "mean_rel": float(r_rho.mean())},
-        "pressure": {"max_rel": float(r_p.max()), "mean_rel": float(r_p.mean())},
+        "pressure": {"max_rel": float(r_p.max()), "mean_rel": float(r_p.mean()),
+                     "max_abs_over_max": float(np.abs(prs.astype(np.float64) - prs64).max() / np.abs(prs64).max())},
         "acceleration": {"max_abs_over_max": float(da.max() / na.max()),
                          "median_rel": float(np.median(da / np.maximum(na, 1e-30))),
                          "max_rel": float((da / np.maximum(na, 1e-30)).max())},
     }
 
 
-def test_dam_break_1m_fields_against_fp64_oracle(gpu_lib, oracle, dam_break):
+@pytest.mark.parametrize("after", [0, 200])
+def test_dam_break_1m_fields_against_fp64_oracle(gpu_lib, oracle, dam_break, after):
+    """FP32 density, pressure and acceleration of one substep against the
+    FP64 restatement on the same sorted input: from the lattice, and from the
+    state the GPU reached after 200 substeps (the column collapsing)."""
     sc = dam_break
-    ref = oracle.step(sc.params, sc.terms, sc.particles, sc.mesh)
+    start = sc.particles
+    if after:
+        with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+            g.upload(sc.particles)
+            g.step(after)
+            assert g.sync() == 0
+            start = g.download()
+    ref = oracle.step(sc.params, sc.terms, start, sc.mesh)
     rho64, prs64, acc64 = oracle.fields_f64(ref.params, ref.sorted, ref.table)
     with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
-        g.upload(sc.particles)
+        g.upload(start)
         g.step_until(STAGE_FORCES)
         rho, prs, acc = g.fields()
         _, perm = g.keys()
     assert np.array_equal(perm, ref.perm)  # the FP64 fields are of the same sorted state
     rep = fp64_report(rho, prs, acc, rho64, prs64, acc64)
-    print("FP32 GPU fields vs FP64 oracle, 1,048,576-particle dam break:", rep)
+    print(f"FP32 GPU fields vs FP64 oracle, 1,048,576-particle dam break after {after} substeps:", rep)
     assert rep["density"]["max_rel"] <= 1e-5
-    assert rep["pressure"]["max_rel"] <= 1e-4
+    assert rep["pressure"]["max_abs_over_max"] <= 1e-5
     assert rep["acceleration"]["max_abs_over_max"] <= 1e-5
     assert rep["acceleration"]["median_rel"] <= 1e-4
 
