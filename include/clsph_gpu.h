@@ -110,9 +110,11 @@ int clsph_gpu_set_collision_cap(clsph_gpu* h, uint32_t max_iterations);
 int clsph_gpu_set_stream(clsph_gpu* h, void* cuda_stream);
 
 /* Replaces the per-substep mesh buffers of sph_simulation.cpp:296-319: the
- * scene (scene.h:11-14 arrays) is uploaded once and indexed by a per-cell
- * triangle list. Face order is kept, so hit selection equals the reference's
- * brute-force loop (collisions.cl:21-87). */
+ * scene (scene.h:11-14 arrays) stays on the device, indexed by a per-cell
+ * triangle list, until it is set again (the host layers set it again when a
+ * callback has changed current_scene). Face order is kept, so hit selection
+ * equals the reference's brute-force loop (collisions.cl:21-87). Synchronises
+ * the handle's stream. */
 int clsph_gpu_set_mesh(clsph_gpu* h, const float* face_normals, const float* vertices,
                        uint32_t vertex_count, const uint32_t* indices, uint32_t face_count);
 /* The mesh of one scene of a batched handle (clsph_gpu_set_mesh = scene 0). */
@@ -152,6 +154,21 @@ int clsph_gpu_step_until(clsph_gpu* h, int stage);
 /* Waits for the stream; *flags (may be NULL) receives the sticky
  * CLSPH_WARN_* bits accumulated since the last call, which are then cleared. */
 int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags);
+
+/* Replaces the parameter block and kernel constants between substeps. The
+ * reference hands `parameters` and `precomputed_terms` to its kernels by value
+ * every substep (sph_simulation.cpp:282-337), so a program that edits them
+ * between substeps (gravity, viscosity, restitution, time step, ...) sees the
+ * change at the next substep; the host layers call this when a callback has
+ * changed them. The particle count of a scene cannot change
+ * (CLSPH_ERR_ARGUMENT: the reference's buffers have a fixed size too); the
+ * grid fields are recomputed every substep and ignored here. The per-cell
+ * triangle lists stay valid for any value (a segment longer than the lists'
+ * reach, which follows from max_velocity and the time step at set_mesh,
+ * tests every face). Synchronises the handle's stream. */
+int clsph_gpu_set_parameters(clsph_gpu* h, const clsph_parameters* params, const clsph_kernel_terms* terms);
+int clsph_gpu_set_scene_parameters(clsph_gpu* h, uint32_t scene, const clsph_parameters* params,
+                                   const clsph_kernel_terms* terms);
 
 /* The parameter block with the grid of the last substep (min_point,
  * max_point, grid_size_*, grid_cell_count), as sph_simulation keeps it. */

@@ -749,6 +749,37 @@ int clsph_gpu_sync(clsph_gpu* h, uint32_t* flags) {
   return CLSPH_OK;
 }
 
+int clsph_gpu_set_scene_parameters(clsph_gpu* h, uint32_t scene, const clsph_parameters* params,
+                                   const clsph_kernel_terms* terms) {
+  if (!h || !params || !terms || scene >= h->nscenes)
+    return fail(CLSPH_ERR_ARGUMENT, "set_parameters: bad argument");
+  const uint32_t count = h->scene_first[scene + 1] - h->scene_first[scene];
+  if (params->particles_count != count)
+    return fail(CLSPH_ERR_ARGUMENT, "set_parameters: the particle count of a scene cannot change");
+  if (!(params->h > 0.f)) return fail(CLSPH_ERR_ARGUMENT, "set_parameters: h must be positive");
+  // kernels of queued substeps read the constants: replace them between substeps
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  clsph_parameters p = *params;
+  const clsph_parameters& old = h->params[scene];
+  // the grid fields are the engine's own, recomputed every substep
+  p.min_point = old.min_point;
+  p.max_point = old.max_point;
+  p.grid_size_x = old.grid_size_x;
+  p.grid_size_y = old.grid_size_y;
+  p.grid_size_z = old.grid_size_z;
+  p.grid_cell_count = old.grid_cell_count;
+  h->params[scene] = p;
+  h->terms[scene] = *terms;
+  h->consts_host[scene] = derive_consts(p, *terms, count);
+  const float hs = p.h;
+  CUDA_TRY(cudaMemcpy(h->scene_h + scene, &hs, sizeof(float), cudaMemcpyHostToDevice));
+  return sync_scene_tables(h);
+}
+
+int clsph_gpu_set_parameters(clsph_gpu* h, const clsph_parameters* params, const clsph_kernel_terms* terms) {
+  return clsph_gpu_set_scene_parameters(h, 0, params, terms);
+}
+
 int clsph_gpu_get_scene_parameters(clsph_gpu* h, uint32_t scene, clsph_parameters* out) {
   if (!h || !out || scene >= h->nscenes) return fail(CLSPH_ERR_ARGUMENT, "get_parameters: bad argument");
   DevGrid g;

@@ -36,6 +36,8 @@ SIGNATURES = [
     ("clsph_gpu_set_scene_mesh", ctypes.c_int, [_vp, _u32, _vp, _vp, _u32, _vp, _u32]),
     ("clsph_gpu_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
     ("clsph_gpu_get_scene_parameters", ctypes.c_int, [_vp, _u32, _vp]),
+    ("clsph_gpu_set_parameters", ctypes.c_int, [_vp, _vp, _vp]),
+    ("clsph_gpu_set_scene_parameters", ctypes.c_int, [_vp, _u32, _vp, _vp]),
     ("clsph_gpu_read_cell_table_scene", ctypes.c_int, [_vp, _u32, _vp, ctypes.c_uint64]),
     ("clsph_gpu_destroy", ctypes.c_int, [_vp]),
     ("clsph_gpu_set_collision_cap", ctypes.c_int, [_vp, _u32]),
@@ -189,6 +191,17 @@ class GpuSolver:
         _check("clsph_gpu_set_scene_mesh",
                self.lib.clsph_gpu_set_scene_mesh(self.h, scene, _a(normals), _a(verts),
                                                  len(verts) // 3, _a(idx), faces))
+
+    def set_parameters(self, params, terms, scene: int = 0) -> None:
+        """Replaces a scene's parameter block and kernel constants between
+        substeps (include/clsph_gpu.h; the particle count cannot change)."""
+        p = np.array(params, dtype=PARAMS).reshape(1).copy()
+        t = np.array(terms, dtype=TERMS).reshape(1).copy()
+        p["particles_count"] = self.counts[scene]
+        _check("clsph_gpu_set_scene_parameters",
+               self.lib.clsph_gpu_set_scene_parameters(self.h, scene, _a(p), _a(t)))
+        self.params[scene] = p[0]
+        self.terms[scene] = t[0]
 
     def set_graph(self, on: bool) -> None:
         _check("clsph_gpu_set_graph", self.lib.clsph_gpu_set_graph(self.h, 1 if on else 0))

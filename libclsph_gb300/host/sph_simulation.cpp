@@ -8,6 +8,7 @@
 // into exit(-1) or assert() are thrown as std::runtime_error.
 
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <fstream>
 #include <iostream>
@@ -157,6 +158,23 @@ void sph_simulation::simulate(int frame_count) {
     up_indices = current_scene.indices;
   };
   if (current_scene.face_count > 0) upload_scene();
+  // The same holds for `parameters` and `precomputed_terms`, which the
+  // reference's kernels receive by value every substep: edits other than to
+  // the grid fields (the engine's own) are handed to the device.
+  auto inputs_of = [&]() {
+    simulation_parameters p = parameters;
+    p.min_point = p.max_point = cl_float3{};
+    p.grid_size_x = p.grid_size_y = p.grid_size_z = p.grid_cell_count = 0;
+    p.constant_acceleration.s[3] = 0.f;  // the padding lane of cl_float3
+    std::vector<unsigned char> b(sizeof(p) + sizeof(precomputed_terms));
+    std::memcpy(b.data(), &p, sizeof(p));
+    std::memcpy(b.data() + sizeof(p), &precomputed_terms, sizeof(precomputed_terms));
+    // the struct's padding before constant_acceleration holds no value
+    const size_t pad0 = offsetof(simulation_parameters, K) + sizeof(p.K);
+    std::memset(b.data() + pad0, 0, offsetof(simulation_parameters, constant_acceleration) - pad0);
+    return b;
+  };
+  std::vector<unsigned char> up_inputs = inputs_of();
   bool scene_check = false;  // a callback ran since the last comparison
   auto refresh_scene = [&]() {
     if (!scene_check) return;
@@ -164,6 +182,15 @@ void sph_simulation::simulate(int frame_count) {
     if (current_scene.face_count != up_faces || current_scene.face_normals != up_normals ||
         current_scene.vertices != up_vertices || current_scene.indices != up_indices)
       upload_scene();
+    std::vector<unsigned char> now = inputs_of();
+    if (now != up_inputs) {
+      if (parameters.particles_count != n)
+        throw std::runtime_error("the particle count cannot change during simulate()");
+      check(clsph_gpu_set_parameters(gpu_, reinterpret_cast<const clsph_parameters*>(&parameters),
+                                     reinterpret_cast<const clsph_kernel_terms*>(&precomputed_terms)),
+            "clsph_gpu_set_parameters");
+      up_inputs.swap(now);
+    }
   };
 
   std::vector<particle> storage(n);

@@ -29,6 +29,8 @@ f32 = np.float32
 
 EVERY_SUBSTEP = "every_substep"
 FRAMES_ONLY = "frames_only"
+# fields of simulation_parameters that the engine recomputes every substep
+GRID_FIELDS = ("min_point", "max_point", "grid_size_x", "grid_size_y", "grid_size_z", "grid_cell_count")
 
 
 def init_lattice(n: int, initial_volume: float) -> np.ndarray:
@@ -88,7 +90,18 @@ class Simulation:
         # (sph_simulation.cpp:296-337), so a callback may edit the scene in
         # place; after a callback the scene is compared with the copy last
         # uploaded and uploaded again when it differs.
-        state = {"device_newer": False, "host_dirty": False, "scene_check": False, "uploaded": None}
+        # The same holds for `parameters` and `precomputed_terms`, which the
+        # reference's kernels receive by value every substep: edits other than
+        # to the grid fields (the engine's own) are handed to the device.
+        state = {"device_newer": False, "host_dirty": False, "scene_check": False, "uploaded": None,
+                 "inputs": None}
+
+        def inputs_copy():
+            prm = np.array(self.parameters, dtype=PARAMS).reshape(1).copy()
+            for f in GRID_FIELDS:
+                prm[f] = 0
+            prm["constant_acceleration"][..., 3] = 0  # the padding lane of cl_float3
+            return prm.tobytes() + np.array(self.precomputed_terms, dtype=TERMS).reshape(1).tobytes()
 
         def scene_copy():
             sc = self.current_scene
@@ -110,12 +123,19 @@ class Simulation:
             if now[0] != up[0] or any(a.shape != b.shape or not np.array_equal(a, b)
                                       for a, b in zip(now[1:], up[1:])):
                 upload_scene(gpu)
+            inputs = inputs_copy()
+            if inputs != state["inputs"]:
+                if int(self.parameters["particles_count"]) != n:
+                    raise RuntimeError("the particle count cannot change during simulate()")
+                gpu.set_parameters(self.parameters, self.precomputed_terms)
+                state["inputs"] = inputs
 
         with GpuSolver(p, self.precomputed_terms, n, None) as gpu:
             if self.current_scene.face_count:
                 upload_scene(gpu)
             else:
                 state["uploaded"] = scene_copy()
+            state["inputs"] = inputs_copy()
             gpu.set_collision_cap(self.collision_iteration_cap)
             gpu.upload(particles)
 
@@ -124,8 +144,7 @@ class Simulation:
                     return
                 gpu.download(particles)
                 grid = gpu.parameters()
-                for f in ("min_point", "max_point", "grid_size_x", "grid_size_y", "grid_size_z",
-                          "grid_cell_count"):
+                for f in GRID_FIELDS:
                     self.parameters[f] = grid[f]
                 flags = gpu.sync()
                 if flags & 1:
@@ -143,12 +162,11 @@ class Simulation:
                 else:
                     cb(particles, self.parameters, full)
 
-            substeps = 0
-            while f32(substeps) < f32(1.0) / f32(p["simulation_scale"]):
-                substeps += 1
             for _ in range(frame_count):
                 call(self.pre_frame, True)
-                for _ in range(substeps):
+                # the loop bound is read every substep, as the reference's is
+                j = 0
+                while f32(j) < f32(1.0) / f32(self.parameters["simulation_scale"]):
                     call(self.pre_frame, False)
                     if state["host_dirty"]:
                         gpu.upload(particles)
@@ -157,6 +175,7 @@ class Simulation:
                     gpu.step(1)
                     state["device_newer"] = True
                     call(self.post_frame, False)
+                    j += 1
                 call(self.post_frame, True)
             refresh()
         self.last_particles = particles

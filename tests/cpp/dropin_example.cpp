@@ -1,9 +1,11 @@
 // A libclsph-style driver written against the drop-in headers: load the two
 // property files and a scene, run `frames` frames with pre/post callbacks,
 // write a Houdini frame and the final particle AoS (raw, like last_frame.bin).
-//   dropin_example <fluid.json> <sim.json> <scene.obj> <frames> <out_prefix> [frames_only|raise_mesh]
+//   dropin_example <fluid.json> <sim.json> <scene.obj> <frames> <out_prefix>
+//                  [frames_only|raise_mesh|flip_gravity]
 // raise_mesh: the 4th substep's pre_frame callback moves every vertex of the
 // scene up by 0.4995 m, in place (the next substeps collide with the moved mesh).
+// flip_gravity: the same callback negates the y gravity in sim.parameters.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -30,6 +32,7 @@ int main(int argc, char** argv) {
   if (argc > 6 && std::string(argv[6]) == "frames_only")
     sim.transfers = sph_simulation::transfer_policy::frames_only;
   const bool raise_mesh = argc > 6 && std::string(argv[6]) == "raise_mesh";
+  const bool flip_gravity = argc > 6 && std::string(argv[6]) == "flip_gravity";
   int substep_calls = 0;
   const std::string prefix = argv[5];
   houdini_file_saver saver(prefix);
@@ -37,8 +40,11 @@ int main(int argc, char** argv) {
   sim.pre_frame = [&](particle* p, const simulation_parameters& prm, bool full) {
     ++pre_calls;
     if (full) saver.writeFrameToFile(p, prm);
-    if (!full && ++substep_calls == 4 && raise_mesh)
-      for (size_t v = 1; v < sim.current_scene.vertices.size(); v += 3) sim.current_scene.vertices[v] += 0.4995f;
+    if (!full && ++substep_calls == 4) {
+      if (raise_mesh)
+        for (size_t v = 1; v < sim.current_scene.vertices.size(); v += 3) sim.current_scene.vertices[v] += 0.4995f;
+      if (flip_gravity) sim.parameters.constant_acceleration.s[1] = -sim.parameters.constant_acceleration.s[1];
+    }
   };
   sim.post_frame = [&](particle* p, const simulation_parameters& prm, bool full) {
     ++post_calls;

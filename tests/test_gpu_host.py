@@ -153,6 +153,51 @@ def test_scene_edits_in_callbacks_reach_the_next_substep(gpu_lib, workdir):
     assert not np.array_equal(moved["position"], still["position"])
 
 
+def flip_gravity_at(sim, substep, calls):
+    def cb(p, prm, full):
+        if not full:
+            calls["n"] += 1
+            if calls["n"] == substep:
+                sim.parameters["constant_acceleration"][1] = -sim.parameters["constant_acceleration"][1]
+    return cb
+
+
+def test_parameter_edits_in_callbacks_reach_the_next_substep(gpu_lib, workdir):
+    """The reference hands `parameters` to its kernels by value every substep
+    (sph_simulation.cpp:282-337), so a callback that edits them (here the
+    gravity) changes the next substeps."""
+    sim = make_sim()
+    calls = {"n": 0}
+    sim.pre_frame = flip_gravity_at(sim, 4, calls)
+    out = sim.simulate(1)
+    assert calls["n"] == 10
+    assert sim.parameters["constant_acceleration"][1] > 0
+    # the engine: 3 substeps under the loaded gravity, 7 under the flipped one
+    base = make_sim()
+    p0 = init_lattice(2744, base.initial_volume)
+    flipped = base.parameters.copy()
+    flipped["constant_acceleration"][1] = -flipped["constant_acceleration"][1]
+    with GpuSolver(base.parameters, base.precomputed_terms, 2744, base.current_scene.mesh()) as g:
+        g.upload(p0)
+        g.step(3)
+        g.set_parameters(flipped, base.precomputed_terms)
+        g.step(7)
+        want = g.download()
+    assert np.array_equal(out.view(np.uint8), want.view(np.uint8))
+    assert not np.array_equal(out["position"], make_sim().simulate(1)["position"])
+
+
+def test_particle_count_edit_is_refused(gpu_lib, workdir):
+    sim = make_sim()
+
+    def shrink(p, prm, full):
+        sim.parameters["particles_count"] = 100
+
+    sim.pre_frame = shrink
+    with pytest.raises(RuntimeError, match="particle count"):
+        sim.simulate(1)
+
+
 def test_frames_only_policy_matches_when_callbacks_only_read(gpu_lib, workdir):
     a = make_sim()
     a.pre_frame = lambda p, prm, full: None
@@ -207,5 +252,14 @@ def test_cpp_dropin_example_matches_python(gpu_lib, workdir):
                 sim.current_scene.vertices[1::3] += RAISE
 
     sim.pre_frame = move_mesh
+    py = sim.simulate(1)
+    assert np.array_equal(cpp.view(np.uint8), py.view(np.uint8))
+    # so do parameters edited by a callback
+    run = subprocess.run([str(exe), "water.json", "sim.json", "cube.obj", "1", "./", "flip_gravity"],
+                         capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr
+    cpp = np.fromfile("final.bin", dtype=PARTICLE)
+    sim = make_sim()
+    sim.pre_frame = flip_gravity_at(sim, 4, {"n": 0})
     py = sim.simulate(1)
     assert np.array_equal(cpp.view(np.uint8), py.view(np.uint8))
