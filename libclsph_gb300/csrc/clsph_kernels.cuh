@@ -994,16 +994,24 @@ __global__ void __launch_bounds__(BLOCK)
 // the 27 cells around it once (lane k < 27: offset k in the reference's z, y,
 // x loop order; also stored as the cell's nb_start row) and holds the cell's
 // particles, two per lane. For each neighbour cell, in that order, that lies
-// in at least one particle's window, it stages the cell's candidates that face
-// the own cell (the far half is skipped by half code), 32 at a time and
-// compacted by ballot, which keeps their sorted order, in shared memory, with
+// in at least one particle's window (the union of the windows as a 27-bit
+// mask), it walks the cell's slots 32 at a time and stages the candidates
+// that face the own cell (the far half is skipped by half code), compacted by
+// ballot, which keeps their sorted order, into a tile in shared memory, with
 // coordinates relative to the own cell's centre and their negated squared
-// norm. A lane tests its particles against each staged candidate with three
-// FMAs, 2 p'.q' - |q'|^2 >= |p'|^2 - R^2 (the squared distance with the
-// particle's part precomputed), sets the candidate's bit in a per-chunk hit
-// mask, and after the chunk appends the hits' tags to the particle's buffer
+// norm. A tile holds up to 32 candidates of one cell: it is tested before a
+// block would overflow it and at the end of its cell, so a cell's facing half
+// of 32 or fewer candidates is one tile however its slots fall into blocks.
+// A lane tests its particles against each staged candidate with three FMAs,
+// 2 p'.q' - |q'|^2 >= |p'|^2 - R^2 (the squared distance with the particle's
+// part precomputed), sets the candidate's bit in the tile's hit mask (the a
+// or b half of the lanes skips a tile whose cell none of its particles
+// needs), and after the tile appends the hits' tags to the particle's buffer
 // in bit order, so each buffer holds the reference's visiting order. The
 // survivors are then evaluated exactly per particle, as in k_density.
+// (Packing the candidates into tiles, instead of testing each 32-slot block
+// on its own, cut the kernel's instructions by 8.5 % and its time by 6-8 %
+// on the 1M dam break.)
 //
 // Rounding of the cull: cell-relative coordinates are within 3h of the
 // centre, so every intermediate of the test is below 50 h^2 and the four
@@ -1039,6 +1047,17 @@ __constant__ OffsetMasks kOffsetMasks = make_offset_masks();
 __device__ __forceinline__ bool near_cull(const float4& p, const float4& q, float r2) {
   const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2;
+}
+
+// The cells of a particle's window as bits k < 27 (z, y, x order): on every
+// axis offset 0, and -1 / +1 where its half code has the lower / upper bit.
+// Bit k is set exactly when (code & own bits of k) == own bits of k.
+__device__ __forceinline__ uint32_t window_cells(uint32_t code) {
+  const uint32_t ax = 2u | (code & 1u) | ((code << 1) & 4u);
+  const uint32_t ay = 2u | ((code >> 2) & 1u) | ((code >> 1) & 4u);
+  const uint32_t az = 2u | ((code >> 4) & 1u) | ((code >> 3) & 4u);
+  const uint32_t yx = ((ay & 1u) ? ax : 0u) | (ax << 3) | ((ay & 4u) ? ax << 6 : 0u);
+  return ((az & 1u) ? yx : 0u) | (yx << 9) | ((az & 4u) ? yx << 18 : 0u);
 }
 
 // survivor buffer per particle: 48 tags (40 with 8 warps, which keeps the
@@ -1103,7 +1122,6 @@ __device__ __forceinline__ void density_cells_warps(
       const float4 pa = va ? pos[ia] : make_float4(0.f, 0.f, 0.f, 0.f);
       const float4 pb = vb ? pos[ib] : make_float4(0.f, 0.f, 0.f, 0.f);
       const uint32_t code_a = __float_as_uint(pa.w), code_b = __float_as_uint(pb.w);
-      const bool two = __any_sync(0xFFFFFFFFu, vb);
       // 2 p' and |p'|^2 - R^2 of both particles
       const float ax = pa.x - ox, ay = pa.y - oy, az = pa.z - oz;
       const float bx = pb.x - ox, by = pb.y - oy, bz = pb.z - oz;
@@ -1112,14 +1130,57 @@ __device__ __forceinline__ void density_cells_warps(
       const float ta = fmaf(ax, ax, fmaf(ay, ay, az * az)) - cull_r2;
       const float tb = fmaf(bx, bx, fmaf(by, by, bz * bz)) - cull_r2;
       uint32_t fa = wide ? kCap + 1u : 0u, fb = fa;
-      for (uint32_t k = 0; k < 27u && !wide; ++k) {
-        const uint32_t masks = kOffsetMasks.m[k];
-        const uint32_t need = masks & 63u;  // the own particle's half toward the cell
-        const uint32_t fm = masks >> 6;     // a candidate's half toward the own cell
+      // the cells of the pass's windows (the union over its particles) in z,
+      // y, x order, each walked in 32-slot blocks; their facing candidates are
+      // packed into tiles of up to 32 of one cell (a tile is tested before a
+      // block would overflow it and at the end of its cell)
+      uint32_t rem = 0;
+      if (!wide)
+        rem = __reduce_or_sync(0xFFFFFFFFu, (va ? window_cells(code_a) : 0u) | (vb ? window_cells(code_b) : 0u));
+      uint32_t nt = 0, kt = 0;  // candidates in the tile, and their cell
+      auto test_tile = [&]() {
+        const uint32_t m = nt;
+        // slots [m, 8 * ceil(m / 8)) hold a candidate no test accepts
+        if (m + lane < ((m + 7u) & ~7u)) stage[wid][m + lane] = make_float4(0.f, 0.f, 0.f, -INFINITY);
+        __syncwarp();
+        const uint32_t need = kOffsetMasks.m[kt] & 63u;  // the own particle's half toward the cell
         const bool na = va && (code_a & need) == need;
         const bool nb = vb && (code_b & need) == need;
-        if (!__any_sync(0xFFFFFFFFu, na || nb)) continue;
         const float tak = na ? ta : INFINITY, tbk = nb ? tb : INFINITY;
+        const bool one = __any_sync(0xFFFFFFFFu, na), two = __any_sync(0xFFFFFFFFu, nb);
+        uint32_t ma = 0, mb = 0;
+        // eight candidates per step, each with its own constant bit
+        for (uint32_t t0 = 0; t0 < m; t0 += 8u) {
+          uint32_t ga = 0, gb = 0;
+#pragma unroll
+          for (uint32_t u = 0; u < 8u; ++u) {
+            const float4 r = stage[wid][t0 + u];
+            if (one && fmaf(a2x, r.x, fmaf(a2y, r.y, fmaf(a2z, r.z, r.w))) >= tak) ga |= 1u << u;
+            if (two && fmaf(b2x, r.x, fmaf(b2y, r.y, fmaf(b2z, r.z, r.w))) >= tbk) gb |= 1u << u;
+          }
+          ma |= ga << t0;
+          mb |= gb << t0;
+        }
+        // hits in candidate order
+        while (ma) {
+          const uint32_t t = __ffs(ma) - 1u;
+          ma &= ma - 1u;
+          if (fa < kCap) cand[wid][fa][lane] = (uint16_t)stag[wid][t];
+          ++fa;
+        }
+        while (mb) {
+          const uint32_t t = __ffs(mb) - 1u;
+          mb &= mb - 1u;
+          if (fb < kCap) cand[wid][fb][lane + 32u] = (uint16_t)stag[wid][t];
+          ++fb;
+        }
+        __syncwarp();
+        nt = 0;
+      };
+      while (rem) {
+        const uint32_t k = __ffs(rem) - 1u;
+        rem &= rem - 1u;
+        const uint32_t fm = (uint32_t)kOffsetMasks.m[k] >> 6;  // a candidate's half toward the own cell
         const uint32_t s = __shfl_sync(0xFFFFFFFFu, nb_s, k), e = __shfl_sync(0xFFFFFFFFu, nb_e, k);
         for (uint32_t cb = s; cb < e; cb += 32u) {
           const uint32_t j = cb + lane;
@@ -1131,43 +1192,18 @@ __device__ __forceinline__ void density_cells_warps(
           }
           const uint32_t bal = __ballot_sync(0xFFFFFFFFu, f);
           const uint32_t cnt = __popc(bal);
+          if (nt + cnt > 32u) test_tile();  // the block would overflow the tile
           if (f) {
-            const uint32_t at = __popc(bal & lt);
+            const uint32_t at = nt + __popc(bal & lt);
             const float qx = q.x - ox, qy = q.y - oy, qz = q.z - oz;
             stage[wid][at] = make_float4(qx, qy, qz, -fmaf(qx, qx, fmaf(qy, qy, qz * qz)));
             stag[wid][at] = (k << kCellOffBits) | (j - s);
           }
-          // slots [cnt, 8 * ceil(cnt / 8)) hold a candidate no test accepts
-          if (cnt + lane < ((cnt + 7u) & ~7u)) stage[wid][cnt + lane] = make_float4(0.f, 0.f, 0.f, -INFINITY);
-          __syncwarp();
-          uint32_t ma = 0, mb = 0;
-          // eight candidates per step, each with its own constant bit
-          for (uint32_t t0 = 0; t0 < cnt; t0 += 8u) {
-            uint32_t ga = 0, gb = 0;
-#pragma unroll
-            for (uint32_t u = 0; u < 8u; ++u) {
-              const float4 r = stage[wid][t0 + u];
-              if (fmaf(a2x, r.x, fmaf(a2y, r.y, fmaf(a2z, r.z, r.w))) >= tak) ga |= 1u << u;
-              if (two && fmaf(b2x, r.x, fmaf(b2y, r.y, fmaf(b2z, r.z, r.w))) >= tbk) gb |= 1u << u;
-            }
-            ma |= ga << t0;
-            mb |= gb << t0;
-          }
-          // hits in candidate order
-          while (ma) {
-            const uint32_t t = __ffs(ma) - 1u;
-            ma &= ma - 1u;
-            if (fa < kCap) cand[wid][fa][lane] = (uint16_t)stag[wid][t];
-            ++fa;
-          }
-          while (mb) {
-            const uint32_t t = __ffs(mb) - 1u;
-            mb &= mb - 1u;
-            if (fb < kCap) cand[wid][fb][lane + 32u] = (uint16_t)stag[wid][t];
-            ++fb;
-          }
-          __syncwarp();
+          nt += cnt;
+          kt = k;
+          if (nt == 32u) test_tile();
         }
+        if (nt) test_tile();  // the end of the cell
       }
       auto finish = [&](uint32_t i, const float4& pi, uint32_t found, uint32_t col) {
         const Consts& c = consts[sc];
