@@ -1222,10 +1222,20 @@ __device__ __forceinline__ void density_cells_warps(
           }
         };
         if (found <= kCap) {
-          for (uint32_t k = 0; k < found; ++k) {
+          // each survivor's position is loaded one survivor ahead
+          auto slot_at = [&](uint32_t k) {
             const uint32_t tag = cand[wid][k][col];
-            const uint32_t j = starts[wid][tag >> kCellOffBits] + (tag & ((1u << kCellOffBits) - 1u));
-            visit(j, __ldg(&pos[j]), tag);
+            return starts[wid][tag >> kCellOffBits] + (tag & ((1u << kCellOffBits) - 1u));
+          };
+          uint32_t tag = found ? (uint32_t)cand[wid][0][col] : 0u;
+          float4 pj = found ? __ldg(&pos[slot_at(0)]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          for (uint32_t k = 0; k < found; ++k) {
+            const uint32_t kn = k + 1 < found ? k + 1 : k;
+            const uint32_t tagn = cand[wid][kn][col];
+            const float4 pn = __ldg(&pos[slot_at(kn)]);
+            visit(0u, pj, tag);
+            tag = tagn;
+            pj = pn;
           }
         } else {
           const Window w = neighbour_window(pi, key, grids[sc]);
