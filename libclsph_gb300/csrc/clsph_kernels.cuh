@@ -999,19 +999,22 @@ __global__ void __launch_bounds__(BLOCK)
 // that face the own cell (the far half is skipped by half code), compacted by
 // ballot, which keeps their sorted order, into a tile in shared memory, with
 // coordinates relative to the own cell's centre and their negated squared
-// norm. A tile holds up to 32 candidates of one cell: it is tested before a
-// block would overflow it and at the end of its cell, so a cell's facing half
-// of 32 or fewer candidates is one tile however its slots fall into blocks.
-// A lane tests its particles against each staged candidate with three FMAs,
-// 2 p'.q' - |q'|^2 >= |p'|^2 - R^2 (the squared distance with the particle's
-// part precomputed), sets the candidate's bit in the tile's hit mask (the a
-// or b half of the lanes skips a tile whose cell none of its particles
-// needs), and after the tile appends the hits' tags to the particle's buffer
-// in bit order, so each buffer holds the reference's visiting order. The
-// survivors are then evaluated exactly per particle, as in k_density.
+// norm. A tile holds up to 32 candidates, of one cell or of consecutive
+// cells: it is tested before a block would overflow it and at the end of the
+// pass. A lane tests both its particles against every staged candidate with
+// three FMAs, 2 p'.q' - |q'|^2 >= |p'|^2 - R^2 (the squared distance with the
+// particle's part precomputed), sets the candidate's bit in the tile's hit
+// mask, and after the tile appends the hits' tags to the particle's buffer in
+// bit order, so each buffer holds the reference's visiting order. A particle
+// also tests candidates of cells outside its own window (those of the other
+// particles' windows); the exact test rejects them, as the reference's walk
+// over all 27 cells does. The survivors are then evaluated exactly per
+// particle, as in k_density.
 // (Packing the candidates into tiles, instead of testing each 32-slot block
 // on its own, cut the kernel's instructions by 8.5 % and its time by 6-8 %
-// on the 1M dam break.)
+// on the 1M dam break; letting tiles span cells, without skipping a half of
+// the lanes whose particles' windows miss the tile's cell, cut another 5 %
+// of the instructions and 4-7 % of the time.)
 //
 // Rounding of the cull: cell-relative coordinates are within 3h of the
 // centre, so every intermediate of the test is below 50 h^2 and the four
@@ -1023,22 +1026,21 @@ __global__ void __launch_bounds__(BLOCK)
 constexpr int kCellWarps = 4;
 constexpr uint32_t kCellOffBits = kTagOffBits;
 
-// Per neighbour offset k (z, y, x order): the half-code bits an own particle
-// needs to face that cell (low 6 bits) and the bits a candidate of that cell
-// needs to face the own cell (next 6 bits), facing_mask(-o) | facing_mask(o) << 6.
+// Per neighbour offset k (z, y, x order): the half-code bits a candidate of
+// that cell needs to face the own cell, facing_mask(o).
 struct OffsetMasks {
-  uint16_t m[27];
+  uint8_t m[27];
 };
 constexpr OffsetMasks make_offset_masks() {
   OffsetMasks t{};
   for (int k = 0; k < 27; ++k) {
     const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
-    uint32_t own = 0, cand = 0;
+    uint32_t cand = 0;
     for (int a = 0; a < 3; ++a) {
-      if (o[a] < 0) { own |= 1u << (2 * a); cand |= 2u << (2 * a); }
-      if (o[a] > 0) { own |= 2u << (2 * a); cand |= 1u << (2 * a); }
+      if (o[a] < 0) cand |= 2u << (2 * a);
+      if (o[a] > 0) cand |= 1u << (2 * a);
     }
-    t.m[k] = (uint16_t)(own | (cand << 6));
+    t.m[k] = (uint8_t)cand;
   }
   return t;
 }
@@ -1051,7 +1053,8 @@ __device__ __forceinline__ bool near_cull(const float4& p, const float4& q, floa
 
 // The cells of a particle's window as bits k < 27 (z, y, x order): on every
 // axis offset 0, and -1 / +1 where its half code has the lower / upper bit.
-// Bit k is set exactly when (code & own bits of k) == own bits of k.
+// Bit k is set exactly when (code & facing_mask(-o)) == facing_mask(-o) for
+// the cell's offset o.
 __device__ __forceinline__ uint32_t window_cells(uint32_t code) {
   const uint32_t ax = 2u | (code & 1u) | ((code << 1) & 4u);
   const uint32_t ay = 2u | ((code >> 2) & 1u) | ((code >> 1) & 4u);
@@ -1132,22 +1135,20 @@ __device__ __forceinline__ void density_cells_warps(
       uint32_t fa = wide ? kCap + 1u : 0u, fb = fa;
       // the cells of the pass's windows (the union over its particles) in z,
       // y, x order, each walked in 32-slot blocks; their facing candidates are
-      // packed into tiles of up to 32 of one cell (a tile is tested before a
-      // block would overflow it and at the end of its cell)
+      // packed into tiles of up to 32 (a tile is tested before a block would
+      // overflow it and at the end of the pass)
       uint32_t rem = 0;
       if (!wide)
         rem = __reduce_or_sync(0xFFFFFFFFu, (va ? window_cells(code_a) : 0u) | (vb ? window_cells(code_b) : 0u));
-      uint32_t nt = 0, kt = 0;  // candidates in the tile, and their cell
+      uint32_t nt = 0;  // candidates in the tile
       auto test_tile = [&]() {
         const uint32_t m = nt;
         // slots [m, 8 * ceil(m / 8)) hold a candidate no test accepts
         if (m + lane < ((m + 7u) & ~7u)) stage[wid][m + lane] = make_float4(0.f, 0.f, 0.f, -INFINITY);
         __syncwarp();
-        const uint32_t need = kOffsetMasks.m[kt] & 63u;  // the own particle's half toward the cell
-        const bool na = va && (code_a & need) == need;
-        const bool nb = vb && (code_b & need) == need;
-        const float tak = na ? ta : INFINITY, tbk = nb ? tb : INFINITY;
-        const bool one = __any_sync(0xFFFFFFFFu, na), two = __any_sync(0xFFFFFFFFu, nb);
+        const float tak = va ? ta : INFINITY, tbk = vb ? tb : INFINITY;
+        // the a or b half of the lanes skips the tile when it holds no particle
+        const bool one = __any_sync(0xFFFFFFFFu, va), two = __any_sync(0xFFFFFFFFu, vb);
         uint32_t ma = 0, mb = 0;
         // eight candidates per step, each with its own constant bit
         for (uint32_t t0 = 0; t0 < m; t0 += 8u) {
@@ -1180,7 +1181,7 @@ __device__ __forceinline__ void density_cells_warps(
       while (rem) {
         const uint32_t k = __ffs(rem) - 1u;
         rem &= rem - 1u;
-        const uint32_t fm = (uint32_t)kOffsetMasks.m[k] >> 6;  // a candidate's half toward the own cell
+        const uint32_t fm = kOffsetMasks.m[k];  // a candidate's half toward the own cell
         const uint32_t s = __shfl_sync(0xFFFFFFFFu, nb_s, k), e = __shfl_sync(0xFFFFFFFFu, nb_e, k);
         for (uint32_t cb = s; cb < e; cb += 32u) {
           const uint32_t j = cb + lane;
@@ -1200,11 +1201,10 @@ __device__ __forceinline__ void density_cells_warps(
             stag[wid][at] = (k << kCellOffBits) | (j - s);
           }
           nt += cnt;
-          kt = k;
           if (nt == 32u) test_tile();
         }
-        if (nt) test_tile();  // the end of the cell
       }
+      if (nt) test_tile();  // the end of the pass
       auto finish = [&](uint32_t i, const float4& pi, uint32_t found, uint32_t col) {
         const Consts& c = consts[sc];
         const float hh = XMUL(c.h, c.h);
