@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from libclsph_gb300 import workloads as W
-from libclsph_gb300.gpu import SEARCH_MODES, STAGE_DENSITY, STAGE_FORCES, GpuSolver
+from libclsph_gb300.gpu import SEARCH_CELL_WARPS, SEARCH_MODES, STAGE_DENSITY, STAGE_FORCES, GpuSolver
 
 pytestmark = pytest.mark.gpu
 
@@ -79,4 +79,49 @@ def test_search_modes_crowded_cell(gpu_lib, oracle, mode):
     ref = oracle.step(scene.params, scene.terms, scene.particles, scene.mesh)
     rho, prs, acc = _fields(scene, mode)
     assert np.array_equal(rho, ref.forces["density"])
+    assert np.array_equal(acc, ref.forces["acceleration"][:, :3])
+
+
+def _random_cloud(n: int, seed: int, per_cell: float = 64.0) -> W.Scene:
+    """n particles placed uniformly at random in a cube sized for a mean of
+    per_cell particles per 2h cell (64 is the lattice's): cell counts scatter
+    around it, so the cell-warp search packs its tiles across cells of ragged
+    sizes and takes second passes for cells above 64."""
+    st = W.water_settings(n)
+    h = float(st.params["h"])
+    side = (n / per_cell) ** (1.0 / 3.0) * 2.0 * h
+    rng = np.random.default_rng(seed)
+    pos = (0.2 + rng.uniform(0.0, side, (n, 3))).astype(np.float32)
+    vel = rng.normal(0.0, 0.2, pos.shape).astype(np.float32)
+    parts = W.particles_from_arrays(pos, vel, vel)
+    return W.Scene(f"cloud_{n}", st.params, st.terms, parts, W.box_mesh((0, 0, 0), (1, 1, 1)), 10, {"h": h})
+
+
+CELL_WARP_SCENES = {
+    # cells of about 48 to 93 particles, 30 neighbours on average
+    "random_cloud": lambda: _random_cloud(8000, seed=17),
+    # about 46 neighbours on average: many particles fill the 8-warp block's
+    # 40-entry survivor buffer and some the 48-entry one of 2/4-warp blocks
+    "dense_cloud": lambda: _random_cloud(8000, seed=18, per_cell=96.0),
+    "mid_planes": lambda: _aligned_block(12),
+}
+
+
+@pytest.mark.parametrize("density_block", [64, 128, 256])
+@pytest.mark.parametrize("name", sorted(CELL_WARP_SCENES))
+def test_cell_warp_blocks_match_oracle(gpu_lib, oracle, name, density_block):
+    """The cell-warp search with 2-, 4- and 8-warp blocks (the 8-warp block's
+    survivor buffer is shorter) against the oracle, on scenes whose cells are
+    ragged, whose particles sit near the buffers' capacity, or on mid-planes."""
+    scene = CELL_WARP_SCENES[name]()
+    ref = oracle.step(scene.params, scene.terms, scene.particles, scene.mesh)
+    with GpuSolver(scene.params, scene.terms, scene.n, scene.mesh) as g:
+        g.set_neighbour_search(SEARCH_CELL_WARPS)
+        g.set_launch_shape(density_block, 128, 8)
+        g.upload(scene.particles)
+        g.step_until(STAGE_FORCES)
+        assert g.sync() == 0
+        rho, prs, acc = g.fields()
+    assert np.array_equal(rho, ref.forces["density"])
+    assert np.array_equal(prs, ref.forces["pressure"])
     assert np.array_equal(acc, ref.forces["acceleration"][:, :3])
