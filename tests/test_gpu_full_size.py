@@ -9,7 +9,9 @@
   131,072-triangle heightfield, whose collisions the oracle cannot run at
   that size).
 * Ten substeps of the 1M dam break against ten oracle substeps (chaotic in
-  the long run, but bit for bit over ten substeps).
+  the long run, but bit for bit over ten substeps), and one substep from the
+  state the GPU reached after 200 substeps against the oracle's substep from
+  that state.
 * The GPU's FP32 density, pressure and acceleration of the 1M dam break
   reported against the FP64 oracle (the same algorithm in double): maximum
   and mean relative error per field, bounded at 1e-5 (density), 1e-4
@@ -69,6 +71,40 @@ def test_dam_break_1m_ten_substeps_match_oracle(gpu_lib, oracle, dam_break):
         assert np.array_equal(out[f][:, :3], want[f][:, :3]), f
     assert np.array_equal(out["density"], want["density"])
     assert np.array_equal(out["pressure"], want["pressure"])
+
+
+@pytest.mark.parametrize("density_block", [128, 256])
+def test_dam_break_1m_collapsed_state_substep_matches_oracle(gpu_lib, oracle, dam_break, density_block):
+    """One substep from the state the GPU reached after 200 substeps (the
+    column collapsing onto the floor: cells of a few to over a hundred
+    particles, second passes and tiles across ragged cells in the cell-warp
+    search), with 4- and 8-warp density blocks, against the oracle's substep
+    from the same state: sort, fields and advected state bit for bit."""
+    sc = dam_break
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.upload(sc.particles)
+        g.step(200)
+        assert g.sync() == 0
+        state = g.download()
+    ref = oracle.step(sc.params, sc.terms, state, sc.mesh)
+    with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+        g.set_launch_shape(density_block, 128, 8)
+        g.upload(state)
+        g.step_until(STAGE_FORCES)
+        rho, prs, acc = g.fields()
+        keys, perm = g.keys()
+        g.upload(state)
+        g.step(1)
+        assert g.sync() == 0
+        out = g.download()
+    assert np.array_equal(perm, ref.perm)
+    assert np.array_equal(keys, ref.sorted["grid_index"])
+    assert np.array_equal(rho, ref.forces["density"])
+    assert np.array_equal(prs, ref.forces["pressure"])
+    assert np.array_equal(acc, ref.forces["acceleration"][:, :3])
+    for f in ("position", "velocity", "intermediate_velocity"):
+        assert np.array_equal(out[f][:, :3], ref.final[f][:, :3]), f
+    assert np.array_equal(out["density"], ref.final["density"])
 
 
 def fp64_report(rho, prs, acc, rho64, prs64, acc64):
