@@ -11,7 +11,6 @@ memory by the tests and scripts). No counterpart in the reference.
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass
 from pathlib import Path
 
 import numpy as np

@@ -4,7 +4,6 @@ frames/substeps/callbacks loop as libclsph/sph_simulation.cpp:346-403."""
 
 import json
 import os
-import shutil
 import subprocess
 from pathlib import Path
 
@@ -14,8 +13,7 @@ import pytest
 from libclsph_gb300 import settings as S
 from libclsph_gb300.gpu import GpuSolver
 from libclsph_gb300.layout import PARTICLE
-from libclsph_gb300.simulation import (EVERY_SUBSTEP, FRAMES_ONLY, HoudiniFileSaver, Simulation,
-                                       init_lattice, save_last_frame)
+from libclsph_gb300.simulation import FRAMES_ONLY, Simulation, init_lattice, save_last_frame
 
 pytestmark = pytest.mark.gpu
 

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from libclsph_gb300 import workloads as W
-from libclsph_gb300.gpu import SEARCH_CELL_WARPS, SEARCH_MODES, STAGE_DENSITY, STAGE_FORCES, GpuSolver
+from libclsph_gb300.gpu import SEARCH_CELL_WARPS, SEARCH_MODES, STAGE_FORCES, GpuSolver
 
 pytestmark = pytest.mark.gpu
 

@@ -4,7 +4,6 @@ reader, the Houdini .geo writer, last_frame.bin, and the C++ host library
 
 import ctypes
 import json
-import os
 from pathlib import Path
 
 import numpy as np

@@ -6,7 +6,6 @@ import multiprocessing as mp
 import os
 import socket
 
-import pytest
 
 SIZES = [2048, 65536, 30000, 4096, 4096, 12000, 9000, 50000, 2100, 33000]
 
