@@ -11,7 +11,7 @@ nearest hit over all faces in face order, a later face winning a tie).
   64 x 64 column cross-section, three layers deep, placed just above the full
   256 x 256-quad heightfield (131,072 triangles plus the 12 of the box) with
   the pour's velocities, over four substeps: keys, order and cell table of the
-  first substep bit-exact, every state within 1e-5 relative.
+  first substep and every state bit for bit.
 
 * the per-cell triangle lists themselves, built on the GPU by
   clsph_gpu_set_scene_mesh, against a numpy restatement of their definition
@@ -37,7 +37,6 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 MESH_CASES = ["monkey_hits", "shower_hits", "labyrinth_hits", "river_hits"]
-RTOL = 1e-5
 
 
 def rel_err(a, b):
@@ -48,10 +47,12 @@ def rel_err(a, b):
 
 
 def assert_same_state(out, want):
+    """Bit for bit; a mismatch reports the largest relative difference."""
     for f in ("position", "velocity", "intermediate_velocity"):
-        assert rel_err(out[f][:, :3], want[f][:, :3]) <= RTOL, f
+        a, b = out[f][:, :3], want[f][:, :3]
+        assert np.array_equal(a, b), f"{f}: max rel diff {rel_err(a, b):.3g}"
     for f in ("density", "pressure"):
-        assert rel_err(out[f], want[f]) <= RTOL, f
+        assert np.array_equal(out[f], want[f]), f"{f}: max rel diff {rel_err(out[f], want[f]):.3g}"
     assert np.array_equal(out["grid_index"], want["grid_index"])
 
 
