@@ -344,11 +344,11 @@ def workload_config(scene, args, n_particles: int | None = None) -> dict:
         "h_m": scene.info.get("h"),
         "scenes": scene.info.get("scenes", 1),
         "faces": len(scene.mesh["indices"]) // 3,
-        "l2": ("inputs larger than L2: a substep moves about 600 B per particle through DRAM "
+        "l2": ("inputs larger than L2: a substep moves about 460 B per particle through DRAM "
                "(neighbour lists, records, state; profiles/dram_bytes_per_particle.json); the GPU "
                "arm also writes a 256 MiB buffer before every timed launch, outside its events")
               if not args.no_flush else
-              "inputs larger than L2: a substep moves about 600 B per particle through DRAM; no flush",
+              "inputs larger than L2: a substep moves about 460 B per particle through DRAM; no flush",
     }
 
 
