@@ -90,9 +90,10 @@ int clsph_host::enqueue_substep(clsph_gpu* h, int until) {
   h->launch(K_GRID_SETUP, k_grid_setup, dim3(1), dim3(256), h->bbox, h->grids,
             (const float*)h->scene_h, h->nscenes, h->status, h->digit_total, h->step_counters,
             h->ctl);
-  CUDA_TRY(cudaMemsetAsync(h->ci.keys, 0, sizeof(uint32_t) * h->slots, h->stream));
+  // k_keys also clears the cell index (slots is a power of two >= 1024)
   h->launch(K_KEYS, k_keys, dim3(blocks), dim3(kBlock), (const float4*)h->st[0].pos, n,
-            (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, h->ctl, h->keys);
+            (const DevGrid*)h->grids, (const uint16_t*)h->scene_of, h->ctl, h->keys,
+            reinterpret_cast<uint4*>(h->ci.keys), h->slots / 4u);
   if (until <= CLSPH_STAGE_GRID) return 0;
   h->launch(K_RADIX_HIST, k_radix_hist, dim3(grid_blocks((n + 3) / 4, h->sm_count * 4)), dim3(kRadixThreads),
             (const uint32_t*)h->keys, n, cctl, h->digit_total, h->lookback, h->ntiles);

@@ -422,11 +422,15 @@ __device__ __forceinline__ void keys_block(uint32_t vb, const float4* __restrict
   if (threadIdx.x == 0) atomicMax(&ctl[kCtlMaxKey], block_max);
 }
 
+// Also clears the cell index for this substep's k_gather (16 bytes a thread,
+// grid-stride), which no kernel between the two reads.
 static __global__ void __launch_bounds__(kBlock)
     k_keys(const float4* __restrict__ pos, uint32_t n, const DevGrid* __restrict__ grids,
            const uint16_t* __restrict__ scene_of, uint32_t* __restrict__ ctl,
-           uint32_t* __restrict__ keys) {
+           uint32_t* __restrict__ keys, uint4* __restrict__ index_keys, uint32_t index_quads) {
   __shared__ uint32_t block_max;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < index_quads; q += gridDim.x * blockDim.x)
+    index_keys[q] = make_uint4(0u, 0u, 0u, 0u);
   keys_block(blockIdx.x, pos, n, grids, scene_of, ctl, keys, block_max);
 }
 
