@@ -67,6 +67,27 @@ def test_batched_scene_matches_oracle(gpu_lib, oracle):
         assert np.array_equal(part["density"], ref["density"])
 
 
+def test_batched_256_full_size_matches_oracle_per_scene(gpu_lib, oracle):
+    """The batched workload at full size: one substep of the 256 dam breaks
+    (4,703,741 particles, per-scene rest density and viscosity, one handle)
+    against the oracle's substep of each scene on its own: every scene's
+    sorted final state, density and pressure bit for bit."""
+    scenes = W.batched_dam_breaks()
+    with GpuSolver.batched([s.params for s in scenes], [s.terms for s in scenes],
+                           [s.n for s in scenes], [s.mesh for s in scenes]) as b:
+        b.upload(np.concatenate([s.particles for s in scenes]))
+        b.step(1)
+        assert b.sync() == 0
+        out = b.download()
+    for k, sc in enumerate(scenes):
+        ref = oracle.step(sc.params, sc.terms, sc.particles, sc.mesh).final
+        part = out[b.first[k]:b.first[k + 1]]
+        for f in ("position", "velocity", "intermediate_velocity"):
+            assert np.array_equal(part[f][:, :3], ref[f][:, :3]), (k, f)
+        assert np.array_equal(part["density"], ref["density"]), k
+        assert np.array_equal(part["pressure"], ref["pressure"]), k
+
+
 @pytest.mark.parametrize("steps", [2, 7, 35])  # 35: two 16-substep replays, one of 2, one launch
 def test_graph_replay_equals_launches(gpu_lib, steps):
     sc = W.small_block(14, seed=70, velocity_sigma=0.4)
