@@ -11,7 +11,8 @@
 * Ten substeps of the 1M dam break against ten oracle substeps (chaotic in
   the long run, but bit for bit over ten substeps), and one substep from the
   state the GPU reached after 200 substeps against the oracle's substep from
-  that state.
+  that state; the 32,768-particle dam break over 100 substeps in every
+  neighbour-search mode.
 * The GPU's FP32 density, pressure and acceleration of the 1M dam break
   reported against the FP64 oracle (the same algorithm in double): maximum
   and mean relative error per field, bounded at 1e-5 (density), 1e-4
@@ -71,6 +72,26 @@ def test_dam_break_1m_ten_substeps_match_oracle(gpu_lib, oracle, dam_break):
         assert np.array_equal(out[f][:, :3], want[f][:, :3]), f
     assert np.array_equal(out["density"], want["density"])
     assert np.array_equal(out["pressure"], want["pressure"])
+
+
+def test_dam_break_32k_hundred_substeps_match_oracle(gpu_lib, oracle):
+    """The 32,768-particle dam break over 100 substeps (the column falling
+    onto the floor of its box, with wall and floor collisions) in every
+    neighbour-search mode against 100 oracle substeps: state, density and
+    pressure bit for bit."""
+    sc = W.dam_break_32k()
+    want = oracle.run(sc.params, sc.terms, sc.particles, 100, sc.mesh)
+    for mode in SEARCH_MODES:
+        with GpuSolver(sc.params, sc.terms, sc.n, sc.mesh) as g:
+            g.set_neighbour_search(mode)
+            g.upload(sc.particles)
+            g.step(100)
+            assert g.sync() == 0
+            out = g.download()
+        for f in ("position", "velocity", "intermediate_velocity"):
+            assert np.array_equal(out[f][:, :3], want[f][:, :3]), (mode, f)
+        assert np.array_equal(out["density"], want["density"]), mode
+        assert np.array_equal(out["pressure"], want["pressure"]), mode
 
 
 @pytest.mark.parametrize("density_block", [128, 256])
