@@ -529,7 +529,8 @@ def main() -> None:
                     help="skip the learned 4x-dt stepper's evaluation on the 1M dam break")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    world, rank, local = dist_setup()
+    # the reference arm runs on the host cores only: its ranks meet over gloo
+    world, rank, local = dist_setup("gloo" if args.impl == "reference" else None)
     if args.impl == "reference":
         run_reference(args, world, rank)
         barrier(world)
